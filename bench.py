@@ -1,0 +1,296 @@
+"""Frame benchmark: 1M-triangle 1920x1080 soup (16x16 bins, depth test on,
+seeded), one frame per step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value   triangles/s of the whole job with the scene resident in HBM (CUDA
+        events around each frame, on the renderer's stream; L2 flushed by a
+        256 MB write before every timed frame, outside the events).
+e2e     the same metric through the C ABI with host buffers: each step
+        copies the vertices from pinned host memory, renders, and reads the
+        framebuffer back into pinned host memory (wall clock per step).
+roofline  the raster kernel (the dominant kernel): algorithmic bytes
+        (4 B per bin entry read + 8 B per pixel written) / its CUDA-event
+        time against the measured HBM copy bandwidth.
+cpu_baseline  the oracle port (CPU restatement of the reference pipeline)
+        on the host cores, one full frame.
+
+--impl reference times that CPU implementation on the same workload.
+Under torchrun each rank renders its own seeded frame (independent
+replicas, weak scaling); rank 0 prints the max-over-ranks line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "custom-gpgpu-rasterizer_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+N_TRI = 1_000_000
+WIDTH, HEIGHT, BIN = 1920, 1080, 16
+METRIC = "triangles/s (1M-tri 1080p soup frame, exact two-pass binning)"
+UNIT = "triangles/s"
+WORKLOAD = "soup-1M-1080p"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(seed: int):
+    import scenes
+    return scenes.soup_scene(N_TRI, WIDTH, HEIGHT, BIN, seed=seed)
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per raster launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "raster_kernel_soup1m_1080p.md")
+    try:
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.e+]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, n in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(scene, threads: int):
+    from oracle import oracle
+    oracle.lib()
+    t0 = time.perf_counter()
+    out = oracle.render(scene, oracle.RASTER_REFERENCE, num_threads=threads, want_bins=False)
+    dt = time.perf_counter() - t0
+    return dt, out
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    scene = make_scene(0)
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt, _ = cpu_baseline(scene, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    t = sum(times) / len(times)
+    value = N_TRI / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": N_TRI, "resolution": [WIDTH, HEIGHT], "bins": [BIN, BIN],
+                       "frames_per_s": 1.0 / t},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "one full frame per step: setup, binning, raster and shading of the 1M soup"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import gbr
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    scene = make_scene(rank)
+    mesh = scene.meshes[0]
+    vbytes = mesh.vertices.nbytes
+    nv = len(mesh.vertices)
+    d_vert = torch.from_numpy(mesh.vertices.view(np.uint8)).to(dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    # device-resident frame ---------------------------------------------------
+    r = gbr.Renderer(WIDTH, HEIGHT)
+    r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, 256)
+    r.bind_mesh_device(d_vert.data_ptr(), nv, mesh.vertex_format)
+    r.set_timing(True)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            r.render_scene(scene, sptr)
+        st = r.stats(sptr)
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    ms_total, ms_setup, ms_bin, ms_raster = [], [], [], []
+    torch.cuda.synchronize(dev)
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            r.render_scene(scene, sptr)
+            st = r.stats(sptr)
+            ms_total.append(st["ms_total"]); ms_setup.append(st["ms_setup"])
+            ms_bin.append(st["ms_bin"]); ms_raster.append(st["ms_raster"])
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    pairs = st["num_pairs"]
+    t_frame = sum(ms_total) / len(ms_total) / 1e3
+    if dist:
+        tt = torch.tensor([t_frame], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_frame = float(tt.item())
+    value = world * N_TRI / t_frame
+    t_raster = sum(ms_raster) / len(ms_raster) / 1e3
+    raster_bytes = 4 * pairs + 8 * WIDTH * HEIGHT
+    frame_bytes = vbytes + 8 * pairs + 8 * WIDTH * HEIGHT
+    peak, peak_kind = measured_peak()
+    achieved = raster_bytes / t_raster / 1e9
+    r.close()
+
+    # end to end through the C ABI with host buffers -----------------------
+    r2 = gbr.Renderer(WIDTH, HEIGHT)
+    r2.load_scene(scene)
+    host_v = torch.from_numpy(mesh.vertices.view(np.uint8).copy()).pin_memory()
+    host_c = torch.empty(WIDTH * HEIGHT, dtype=torch.int32).pin_memory()
+    colour_np = host_c.numpy().view(np.uint32)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            r2.update_vertices(0, host_v.data_ptr(), nv, sptr)
+            r2.render_scene(scene, sptr)
+            r2.readback(colour_np, stream=sptr, want_depth=False)
+    if dist:
+        dist.barrier()
+    e2e_times = []
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            r2.update_vertices(0, host_v.data_ptr(), nv, sptr)
+            r2.render_scene(scene, sptr)
+            r2.readback(colour_np, stream=sptr, want_depth=False)
+            e2e_times.append(time.perf_counter() - t0)
+    t_e2e = sum(e2e_times) / len(e2e_times)
+    if dist:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    r2.close()
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            dt, _ = cpu_baseline(scene, threads)
+            cpu = {"value": N_TRI / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "one full frame of the same 1M soup (setup, binning, raster, shading)"}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_frame * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded soup per rank)",
+                "config": {"workload": WORKLOAD, "triangles": N_TRI, "resolution": [WIDTH, HEIGHT],
+                           "bins": [BIN, BIN], "queue_chunk": 256, "binning": "exact two-pass",
+                           "l2": "256 MB write between timed frames", "pairs": int(pairs),
+                           "frames_per_s": world / t_frame,
+                           "ms_setup": statistics.mean(ms_setup), "ms_bin": statistics.mean(ms_bin),
+                           "ms_raster": statistics.mean(ms_raster),
+                           "frame_hbm_frac": frame_bytes / t_frame / 1e9 / peak},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": profile_traffic(), "kernel": "raster_kernel",
+                             "peak_source": peak_kind, "algorithmic_bytes_per_launch": raster_bytes},
+                "e2e": {"value": world * N_TRI / t_e2e, "unit": UNIT, "h2d_bytes_per_step": vbytes,
+                        "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
+                "gpu_launches": 4 * args.steps,
+                "clocks": clocks,
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import build as gbr_build
+    if rank == 0:
+        gbr_build.build()
+    else:
+        while not gbr_build.up_to_date():
+            time.sleep(1)
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,654 @@
+// gbr_api.cu -- C ABI (include/gbr.h) over the frame kernels.
+//
+// Host orchestration of one frame, replacing CUDARenderer::Render's
+// per-mesh loop, its per-256-triangle chunk loop and the device-wide
+// synchronisation after every stage (CustomCUDARasterizer/CUDARenderer.cu:
+// 206-354): a frame is four kernel launches on the caller's stream with no
+// host synchronisation, whatever the number of meshes or triangles.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gbr.h"
+#include "gbr_kernels.h"
+
+using namespace gbr;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gbr_status fail(gbr_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define GBR_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return fail(GBR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+struct MeshHost {
+    bool owned = false;
+    void* d_vertices = nullptr;
+    uint32_t* d_indices = nullptr;
+    uint32_t num_vertices = 0, num_indices = 0, vertex_format = 0, topology = 0;
+    uint64_t num_tris = 0;
+    float world[16];
+    int32_t tex_ids[4] = {-1, -1, -1, -1};
+};
+
+struct TexHost {
+    uint32_t* d_px = nullptr;
+    uint32_t w = 0, h = 0;
+};
+
+uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_indices, uint32_t topology) {
+    if (!indices) return num_vertices / 3u;
+    if (topology == GBR_TOPOLOGY_TRIANGLE_LIST) return num_indices / 3u;
+    return num_indices >= 2u ? num_indices - 2u : 0u;
+}
+
+// Matrix<4,4>::operator*(Matrix<4,4>) (Matrix4.h:120-143) on the host, left
+// to right with no fused multiply-add (built with -ffp-contract=off), as the
+// reference computes WVP.
+void mat4_mul(const float* lm, const float* rm, float* out) {
+    float t[16];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            float s = lm[0 * 4 + r] * rm[c * 4 + 0];
+            s = s + lm[1 * 4 + r] * rm[c * 4 + 1];
+            s = s + lm[2 * 4 + r] * rm[c * 4 + 2];
+            s = s + lm[3 * 4 + r] * rm[c * 4 + 3];
+            t[c * 4 + r] = s;
+        }
+    memcpy(out, t, sizeof t);
+}
+
+}  // namespace
+
+struct gbr_renderer {
+    int device = 0;
+    int num_sms = 0;
+    uint32_t W = 0, H = 0;
+    uint32_t nbx = 0, nby = 0, bw = 0, bh = 0, chunk = 256;
+    bool bins_ready = false;
+    uint32_t binning = GBR_BINNING_EXACT;
+    bool timing = false;
+    int raster_blocks_per_sm = 1;
+
+    std::vector<MeshHost> meshes;
+    std::vector<TexHost> textures;
+
+    uint32_t* d_colour = nullptr;
+    float* d_depth = nullptr;
+    uint32_t* d_ids = nullptr;
+    unsigned long long* d_gvis = nullptr;
+
+    uint32_t* d_counts = nullptr;
+    uint32_t* d_offsets = nullptr;
+    uint32_t* d_cursors = nullptr;
+    uint32_t* d_capacity = nullptr;
+    uint32_t* d_bin_done = nullptr;
+    uint4* d_items = nullptr;
+    uint32_t items_cap = 0;
+    uint32_t* d_list = nullptr;
+    uint64_t list_cap = 0;
+
+    TriSetup* d_setup = nullptr;
+    uint2* d_rects = nullptr;
+    uint64_t tri_cap = 0;
+
+    MeshDev* d_meshes = nullptr;
+    MeshDev* h_meshes = nullptr;
+    uint32_t meshes_cap = 0;
+    std::vector<MeshDev> last_uploaded;
+    cudaEvent_t meshes_evt = nullptr;
+
+    Ctl* d_ctl = nullptr;
+    Ctl* h_ctl = nullptr;
+
+    bool have_frame = false;
+    gbr_camera last_cam{};
+    uint32_t last_cull = 0, last_sample = 0, last_vis = 0;
+    uint32_t overflow_reruns = 0;
+    cudaEvent_t ev[5] = {};
+    bool ev_recorded = false;
+};
+
+namespace {
+
+void free_bins(gbr_renderer* r) {
+    cudaFree(r->d_counts); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
+    cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list);
+    r->d_counts = r->d_offsets = r->d_cursors = r->d_capacity = r->d_bin_done = r->d_list = nullptr;
+    r->d_items = nullptr;
+    r->items_cap = 0;
+    r->list_cap = 0;
+}
+
+gbr_status ensure_list(gbr_renderer* r, uint64_t pairs) {
+    const uint32_t nb = r->nbx * r->nby;
+    if (pairs <= r->list_cap && r->d_list) return GBR_OK;
+    uint64_t cap = std::max<uint64_t>(pairs + pairs / 4u, 1u << 20);
+    if (cap > 0x7FFFFFFFull) cap = 0x7FFFFFFFull;
+    if (pairs > cap) return fail(GBR_ERR_OUT_OF_MEMORY, "frame needs %llu bin entries (max 2^31-1)", (unsigned long long)pairs);
+    cudaFree(r->d_list);
+    cudaFree(r->d_items);
+    r->d_list = nullptr;
+    r->d_items = nullptr;
+    const uint64_t items = (uint64_t)nb + cap / r->chunk + 1u;
+    if (cudaMalloc(&r->d_list, cap * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&r->d_items, items * sizeof(uint4)) != cudaSuccess) {
+        cudaGetLastError();
+        r->list_cap = 0;
+        r->items_cap = 0;
+        return fail(GBR_ERR_OUT_OF_MEMORY, "cannot allocate %llu bin entries", (unsigned long long)cap);
+    }
+    r->list_cap = cap;
+    r->items_cap = (uint32_t)std::min<uint64_t>(items, 0xFFFFFFFFull);
+    return GBR_OK;
+}
+
+gbr_status ensure_tris(gbr_renderer* r, uint64_t tris) {
+    if (tris <= r->tri_cap && r->d_setup) return GBR_OK;
+    cudaFree(r->d_setup);
+    cudaFree(r->d_rects);
+    r->d_setup = nullptr;
+    r->d_rects = nullptr;
+    const uint64_t cap = std::max<uint64_t>(tris, 1024u);
+    if (cudaMalloc(&r->d_setup, cap * sizeof(TriSetup)) != cudaSuccess ||
+        cudaMalloc(&r->d_rects, cap * sizeof(uint2)) != cudaSuccess) {
+        cudaGetLastError();
+        r->tri_cap = 0;
+        return fail(GBR_ERR_OUT_OF_MEMORY, "cannot allocate setup records for %llu triangles", (unsigned long long)tris);
+    }
+    r->tri_cap = cap;
+    return GBR_OK;
+}
+
+gbr_status ensure_meshes(gbr_renderer* r, uint32_t n) {
+    if (n <= r->meshes_cap && r->d_meshes) return GBR_OK;
+    if (r->meshes_evt) cudaEventSynchronize(r->meshes_evt);
+    cudaFree(r->d_meshes);
+    cudaFreeHost(r->h_meshes);
+    r->d_meshes = nullptr;
+    r->h_meshes = nullptr;
+    const uint32_t cap = std::max<uint32_t>(n, 16u);
+    GBR_CUDA(cudaMalloc(&r->d_meshes, cap * sizeof(MeshDev)));
+    GBR_CUDA(cudaMallocHost(&r->h_meshes, cap * sizeof(MeshDev)));
+    r->meshes_cap = cap;
+    r->last_uploaded.clear();
+    return GBR_OK;
+}
+
+TexDev tex_dev(const gbr_renderer* r, int32_t id) {
+    TexDev t{nullptr, 0u, 0u};
+    if (id >= 0 && (size_t)id < r->textures.size() && r->textures[id].d_px) {
+        t.px = r->textures[id].d_px;
+        t.w = r->textures[id].w;
+        t.h = r->textures[id].h;
+    }
+    return t;
+}
+
+gbr_status validate_mesh_args(const void* vertices, uint32_t num_vertices, uint32_t vertex_format,
+                              const uint32_t* indices, uint32_t num_indices, uint32_t topology, const float* world) {
+    if (!vertices && num_vertices) return fail(GBR_ERR_INVALID_ARG, "vertices is null");
+    if (vertex_format > GBR_VERTEX_POS3_RGBA8) return fail(GBR_ERR_INVALID_ARG, "unknown vertex format %u", vertex_format);
+    if (topology > GBR_TOPOLOGY_TRIANGLE_STRIP) return fail(GBR_ERR_INVALID_ARG, "unknown topology %u", topology);
+    if (!indices && topology != GBR_TOPOLOGY_TRIANGLE_LIST)
+        return fail(GBR_ERR_INVALID_ARG, "a triangle strip needs an index buffer");
+    if (!world) return fail(GBR_ERR_INVALID_ARG, "world matrix is null");
+    (void)num_indices;
+    return GBR_OK;
+}
+
+// Renders one frame on `s` (no host synchronisation).
+gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, uint32_t sample, uint32_t vis,
+                        cudaStream_t s) {
+    const uint32_t nb = r->nbx * r->nby;
+    uint64_t ntris = 0;
+    for (const MeshHost& m : r->meshes) ntris += m.num_tris;
+    if (ntris >= 0x7FFFFFFFull) return fail(GBR_ERR_INVALID_ARG, "too many triangles (%llu)", (unsigned long long)ntris);
+    gbr_status st = ensure_tris(r, ntris);
+    if (st != GBR_OK) return st;
+    st = ensure_list(r, std::max<uint64_t>(r->list_cap, 8u * ntris));
+    if (st != GBR_OK) return st;
+    st = ensure_meshes(r, (uint32_t)r->meshes.size());
+    if (st != GBR_OK) return st;
+
+    // per-mesh descriptors with the matrices of this frame
+    float vp[16];
+    mat4_mul(cam->proj, cam->view, vp);
+    std::vector<MeshDev> md(r->meshes.size());
+    uint32_t base = 0;
+    for (size_t i = 0; i < r->meshes.size(); ++i) {
+        const MeshHost& m = r->meshes[i];
+        MeshDev& d = md[i];
+        memset(&d, 0, sizeof d);
+        d.vertices = m.d_vertices;
+        d.indices = m.d_indices;
+        d.vertex_format = m.vertex_format;
+        d.topology = m.topology;
+        d.num_vertices = m.num_vertices;
+        d.num_tris = (uint32_t)m.num_tris;
+        d.prim_base = base;
+        base += (uint32_t)m.num_tris;
+        mat4_mul(vp, m.world, d.wvp);
+        memcpy(d.world, m.world, sizeof d.world);
+        // UpdateCUDAMeshTextures (CUDARenderer.cu:549-573): normal needs
+        // diffuse; specular and gloss need normal
+        const TexDev diff = tex_dev(r, m.tex_ids[0]);
+        if (diff.px) {
+            d.tex[0] = diff;
+            const TexDev norm = tex_dev(r, m.tex_ids[1]);
+            if (norm.px) {
+                d.tex[1] = norm;
+                d.tex[2] = tex_dev(r, m.tex_ids[2]);
+                d.tex[3] = tex_dev(r, m.tex_ids[3]);
+            }
+        }
+    }
+    const bool same = md.size() == r->last_uploaded.size() &&
+                      (md.empty() || memcmp(md.data(), r->last_uploaded.data(), md.size() * sizeof(MeshDev)) == 0);
+    if (!same && !md.empty()) {
+        GBR_CUDA(cudaEventSynchronize(r->meshes_evt));  // previous copy out of the staging buffer is done
+        memcpy(r->h_meshes, md.data(), md.size() * sizeof(MeshDev));
+        GBR_CUDA(cudaMemcpyAsync(r->d_meshes, r->h_meshes, md.size() * sizeof(MeshDev), cudaMemcpyHostToDevice, s));
+        GBR_CUDA(cudaEventRecord(r->meshes_evt, s));
+        r->last_uploaded = md;
+    }
+
+    FrameDev F;
+    memset(&F, 0, sizeof F);
+    F.width = r->W; F.height = r->H;
+    F.nbx = r->nbx; F.nby = r->nby; F.bw = r->bw; F.bh = r->bh; F.num_bins = nb;
+    F.cull = cull; F.sample = sample; F.vis = vis; F.clear_colour32 = 0x003F3F3Fu;
+    F.num_meshes = (uint32_t)r->meshes.size();
+    F.num_tris = (uint32_t)ntris;
+    F.chunk = r->chunk;
+    for (int k = 0; k < 3; ++k) { F.cam_pos[k] = cam->pos[k]; F.cam_fwd[k] = cam->fwd[k]; }
+    F.meshes = r->d_meshes;
+    F.setup = r->d_setup; F.rects = r->d_rects;
+    F.counts = r->d_counts; F.offsets = r->d_offsets; F.cursors = r->d_cursors; F.capacity = r->d_capacity;
+    F.bin_done = r->d_bin_done;
+    F.items = r->d_items; F.items_cap = r->items_cap;
+    F.list = r->d_list; F.list_cap = r->list_cap;
+    F.colour = r->d_colour; F.depth = r->d_depth; F.ids = r->d_ids; F.gvis = r->d_gvis;
+    F.ctl = r->d_ctl;
+
+    if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[0], s));
+    GBR_CUDA(cudaMemsetAsync(r->d_ctl, 0, sizeof(Ctl), s));
+    if ((uint64_t)r->nbx * r->bw < r->W || (uint64_t)r->nby * r->bh < r->H) GBR_CUDA(launch_clear(F, s));
+    GBR_CUDA(launch_setup(F, false, s));
+    if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
+    GBR_CUDA(launch_scan(F, false, s));
+    GBR_CUDA(launch_fill(F, s));
+    if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[2], s));
+    GBR_CUDA(launch_raster(F, (uint32_t)(r->num_sms * r->raster_blocks_per_sm), s));
+    if (r->timing) {
+        GBR_CUDA(cudaEventRecord(r->ev[3], s));
+        r->ev_recorded = true;
+    }
+    r->have_frame = true;
+    r->last_cam = *cam;
+    r->last_cull = cull; r->last_sample = sample; r->last_vis = vis;
+    return GBR_OK;
+}
+
+// Waits for the stream; re-renders with larger bin storage if the frame
+// overflowed it.
+gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
+    GBR_CUDA(cudaStreamSynchronize(s));
+    GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    for (int attempt = 0; r->h_ctl->overflow && attempt < 3; ++attempt) {
+        const uint64_t need = r->h_ctl->num_pairs;
+        gbr_status st = ensure_list(r, need);
+        if (st != GBR_OK) return st;
+        ++r->overflow_reruns;
+        st = render_frame(r, &r->last_cam, r->last_cull, r->last_sample, r->last_vis, s);
+        if (st != GBR_OK) return st;
+        GBR_CUDA(cudaStreamSynchronize(s));
+        GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    }
+    if (r->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "bin storage overflow persists");
+    return GBR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbr_last_error_string(void) { return g_last_error.c_str(); }
+
+uint32_t gbr_version(void) { return 0x000100u; }
+
+gbr_status gbr_create(uint32_t width, uint32_t height, gbr_renderer** out) {
+    if (!out) return fail(GBR_ERR_INVALID_ARG, "out is null");
+    *out = nullptr;
+    if (width == 0 || height == 0 || width > 8192u || height > 8192u)
+        return fail(GBR_ERR_INVALID_ARG, "resolution %ux%u outside 1..8192", width, height);
+    gbr_renderer* r = new (std::nothrow) gbr_renderer();
+    if (!r) return fail(GBR_ERR_OUT_OF_MEMORY, "host allocation failed");
+    r->W = width;
+    r->H = height;
+    cudaError_t e = cudaGetDevice(&r->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&r->num_sms, cudaDevAttrMultiProcessorCount, r->device);
+    const size_t npx = (size_t)width * height;
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_colour, npx * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_depth, npx * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_ids, npx * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_gvis, npx * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(r->d_gvis, 0xFF, npx * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(r->d_colour, 0, npx * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(r->d_depth, 0, npx * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(r->d_ids, 0xFF, npx * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_ctl, sizeof(Ctl));
+    if (e == cudaSuccess) e = cudaMemset(r->d_ctl, 0, sizeof(Ctl));
+    if (e == cudaSuccess) e = cudaMallocHost(&r->h_ctl, sizeof(Ctl));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->meshes_evt, cudaEventDisableTiming);
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&r->ev[i]);
+    if (e != cudaSuccess) {
+        gbr_destroy(r);
+        return fail(GBR_ERR_CUDA, "gbr_create: %s", cudaGetErrorString(e));
+    }
+    *out = r;
+    return GBR_OK;
+}
+
+gbr_status gbr_destroy(gbr_renderer* r) {
+    if (!r) return GBR_OK;
+    cudaDeviceSynchronize();
+    gbr_scene_clear(r);
+    for (TexHost& t : r->textures) cudaFree(t.d_px);
+    free_bins(r);
+    cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis);
+    cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_meshes); cudaFree(r->d_ctl);
+    cudaFreeHost(r->h_meshes); cudaFreeHost(r->h_ctl);
+    if (r->meshes_evt) cudaEventDestroy(r->meshes_evt);
+    for (int i = 0; i < 5; ++i)
+        if (r->ev[i]) cudaEventDestroy(r->ev[i]);
+    delete r;
+    return GBR_OK;
+}
+
+gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bins_y, uint32_t bin_w, uint32_t bin_h,
+                          uint32_t queue_chunk) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    if (num_bins_x == 0 || num_bins_y == 0 || bin_w == 0 || bin_h == 0 || bin_w > (uint32_t)kMaxBinDim ||
+        bin_h > (uint32_t)kMaxBinDim)
+        return fail(GBR_ERR_INVALID_ARG, "bins %ux%u of %ux%u px: need >= 1 bin of 1..%d px", num_bins_x, num_bins_y,
+                    bin_w, bin_h, kMaxBinDim);
+    if (num_bins_x > 32767u || num_bins_y > 32767u) return fail(GBR_ERR_INVALID_ARG, "too many bins");
+    if (queue_chunk == 0) queue_chunk = 256;
+    cudaDeviceSynchronize();
+    free_bins(r);
+    r->nbx = num_bins_x; r->nby = num_bins_y; r->bw = bin_w; r->bh = bin_h; r->chunk = queue_chunk;
+    const uint32_t nb = num_bins_x * num_bins_y;
+    GBR_CUDA(cudaMalloc(&r->d_counts, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_counts, 0, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_offsets, (nb + 1u) * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_offsets, 0, (nb + 1u) * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_cursors, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_capacity, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_capacity, 0, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_bin_done, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_bin_done, 0, nb * sizeof(uint32_t)));
+    int bps = 0;
+    GBR_CUDA(raster_configure(bin_w, bin_h, &bps));
+    r->raster_blocks_per_sm = std::max(bps, 1);
+    r->bins_ready = true;
+    r->have_frame = false;
+    return GBR_OK;
+}
+
+static gbr_status add_mesh(gbr_renderer* r, MeshHost&& m, uint32_t* mesh_id) {
+    r->meshes.push_back(std::move(m));
+    if (mesh_id) *mesh_id = (uint32_t)r->meshes.size() - 1u;
+    return GBR_OK;
+}
+
+gbr_status gbr_mesh_upload(gbr_renderer* r, const void* vertices, uint32_t num_vertices, uint32_t vertex_format,
+                           const uint32_t* indices, uint32_t num_indices, uint32_t topology, const float world[16],
+                           const int32_t tex_ids[4], uint32_t* mesh_id) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    gbr_status st = validate_mesh_args(vertices, num_vertices, vertex_format, indices, num_indices, topology, world);
+    if (st != GBR_OK) return st;
+    MeshHost m;
+    m.owned = true;
+    m.num_vertices = num_vertices;
+    m.num_indices = indices ? num_indices : 0u;
+    m.vertex_format = vertex_format;
+    m.topology = topology;
+    m.num_tris = tri_count(num_vertices, indices, num_indices, topology);
+    memcpy(m.world, world, sizeof m.world);
+    if (tex_ids) memcpy(m.tex_ids, tex_ids, sizeof m.tex_ids);
+    if (indices) {
+        for (uint32_t i = 0; i < num_indices; ++i)
+            if (indices[i] >= num_vertices)
+                return fail(GBR_ERR_INVALID_ARG, "index %u at position %u is out of range (%u vertices)", indices[i], i,
+                            num_vertices);
+    }
+    const size_t vbytes = (size_t)num_vertices * (vertex_format == GBR_VERTEX_IVERTEX56 ? 56u : 16u);
+    if (vbytes) {
+        GBR_CUDA(cudaMalloc(&m.d_vertices, vbytes));
+        GBR_CUDA(cudaMemcpy(m.d_vertices, vertices, vbytes, cudaMemcpyHostToDevice));
+    }
+    if (indices && num_indices) {
+        cudaError_t e = cudaMalloc(&m.d_indices, (size_t)num_indices * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemcpy(m.d_indices, indices, (size_t)num_indices * 4u, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(m.d_vertices);
+            return fail(GBR_ERR_CUDA, "index upload: %s", cudaGetErrorString(e));
+        }
+    }
+    return add_mesh(r, std::move(m), mesh_id);
+}
+
+gbr_status gbr_mesh_update_vertices(gbr_renderer* r, uint32_t mesh_id, const void* vertices, uint32_t num_vertices,
+                                    void* stream) {
+    if (!r || mesh_id >= r->meshes.size()) return fail(GBR_ERR_INVALID_ARG, "bad renderer or mesh id");
+    MeshHost& m = r->meshes[mesh_id];
+    if (!m.owned) return fail(GBR_ERR_INVALID_ARG, "mesh %u is bound to caller memory", mesh_id);
+    if (num_vertices != m.num_vertices || !vertices)
+        return fail(GBR_ERR_INVALID_ARG, "vertex count %u differs from the mesh's %u", num_vertices, m.num_vertices);
+    const size_t vbytes = (size_t)num_vertices * (m.vertex_format == GBR_VERTEX_IVERTEX56 ? 56u : 16u);
+    GBR_CUDA(cudaMemcpyAsync(m.d_vertices, vertices, vbytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return GBR_OK;
+}
+
+gbr_status gbr_mesh_bind_device(gbr_renderer* r, const void* d_vertices, uint32_t num_vertices, uint32_t vertex_format,
+                                const uint32_t* d_indices, uint32_t num_indices, uint32_t topology,
+                                const float world[16], const int32_t tex_ids[4], uint32_t* mesh_id) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    gbr_status st = validate_mesh_args(d_vertices, num_vertices, vertex_format, d_indices, num_indices, topology, world);
+    if (st != GBR_OK) return st;
+    if (vertex_format == GBR_VERTEX_POS3_RGBA8 && ((uintptr_t)d_vertices & 15u))
+        return fail(GBR_ERR_INVALID_ARG, "compact vertices must be 16-byte aligned");
+    MeshHost m;
+    m.owned = false;
+    m.d_vertices = const_cast<void*>(d_vertices);
+    m.d_indices = const_cast<uint32_t*>(d_indices);
+    m.num_vertices = num_vertices;
+    m.num_indices = d_indices ? num_indices : 0u;
+    m.vertex_format = vertex_format;
+    m.topology = topology;
+    m.num_tris = tri_count(num_vertices, d_indices, num_indices, topology);
+    memcpy(m.world, world, sizeof m.world);
+    if (tex_ids) memcpy(m.tex_ids, tex_ids, sizeof m.tex_ids);
+    return add_mesh(r, std::move(m), mesh_id);
+}
+
+gbr_status gbr_mesh_set_world(gbr_renderer* r, uint32_t mesh_id, const float world[16]) {
+    if (!r || mesh_id >= r->meshes.size() || !world) return fail(GBR_ERR_INVALID_ARG, "bad renderer, mesh id or matrix");
+    memcpy(r->meshes[mesh_id].world, world, 16 * sizeof(float));
+    return GBR_OK;
+}
+
+gbr_status gbr_mesh_set_textures(gbr_renderer* r, uint32_t mesh_id, const int32_t tex_ids[4]) {
+    if (!r || mesh_id >= r->meshes.size() || !tex_ids) return fail(GBR_ERR_INVALID_ARG, "bad renderer, mesh id or ids");
+    memcpy(r->meshes[mesh_id].tex_ids, tex_ids, 4 * sizeof(int32_t));
+    return GBR_OK;
+}
+
+gbr_status gbr_scene_clear(gbr_renderer* r) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    cudaDeviceSynchronize();
+    for (MeshHost& m : r->meshes)
+        if (m.owned) {
+            cudaFree(m.d_vertices);
+            cudaFree(m.d_indices);
+        }
+    r->meshes.clear();
+    r->last_uploaded.clear();
+    r->have_frame = false;
+    return GBR_OK;
+}
+
+gbr_status gbr_texture_upload(gbr_renderer* r, const uint32_t* rgba8, uint32_t w, uint32_t h, int32_t* tex_id) {
+    if (!r || !rgba8 || !tex_id) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    if (w == 0 || h == 0 || (uint64_t)w * h > 0x7FFFFFFFull) return fail(GBR_ERR_INVALID_ARG, "texture %ux%u", w, h);
+    TexHost t;
+    t.w = w;
+    t.h = h;
+    GBR_CUDA(cudaMalloc(&t.d_px, (size_t)w * h * 4u));
+    cudaError_t e = cudaMemcpy(t.d_px, rgba8, (size_t)w * h * 4u, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(t.d_px);
+        return fail(GBR_ERR_CUDA, "texture upload: %s", cudaGetErrorString(e));
+    }
+    r->textures.push_back(t);
+    *tex_id = (int32_t)r->textures.size() - 1;
+    r->last_uploaded.clear();
+    return GBR_OK;
+}
+
+gbr_status gbr_texture_remove(gbr_renderer* r, int32_t tex_id) {
+    if (!r || tex_id < 0 || (size_t)tex_id >= r->textures.size() || !r->textures[tex_id].d_px)
+        return fail(GBR_ERR_NOT_FOUND, "texture %d does not exist", tex_id);
+    cudaDeviceSynchronize();
+    cudaFree(r->textures[tex_id].d_px);
+    r->textures[tex_id] = TexHost();
+    r->last_uploaded.clear();
+    return GBR_OK;
+}
+
+gbr_status gbr_set_binning(gbr_renderer* r, uint32_t method) {
+    if (!r || method > GBR_BINNING_PREDICTED) return fail(GBR_ERR_INVALID_ARG, "bad renderer or binning method");
+    r->binning = method;
+    return GBR_OK;
+}
+
+gbr_status gbr_set_bin_capacity(gbr_renderer* r, const uint32_t* capacity, int is_device, void* stream) {
+    if (!r || !capacity || !r->bins_ready) return fail(GBR_ERR_INVALID_ARG, "bins not set up or null capacity");
+    const size_t bytes = (size_t)r->nbx * r->nby * sizeof(uint32_t);
+    GBR_CUDA(cudaMemcpyAsync(r->d_capacity, capacity, bytes, is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             (cudaStream_t)stream));
+    return GBR_OK;
+}
+
+gbr_status gbr_set_timing(gbr_renderer* r, int enabled) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    r->timing = enabled != 0;
+    return GBR_OK;
+}
+
+gbr_status gbr_render(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, uint32_t sample, uint32_t vis,
+                      void* stream) {
+    if (!r || !cam) return fail(GBR_ERR_INVALID_ARG, "null renderer or camera");
+    if (!r->bins_ready) return fail(GBR_ERR_INVALID_ARG, "gbr_setup_bins was not called");
+    if (cull > GBR_CULL_NONE || sample > GBR_SAMPLE_LINEAR || vis > GBR_VIS_NORMAL)
+        return fail(GBR_ERR_INVALID_ARG, "bad cull/sample/vis (%u/%u/%u)", cull, sample, vis);
+    return render_frame(r, cam, cull, sample, vis, (cudaStream_t)stream);
+}
+
+gbr_status gbr_readback(gbr_renderer* r, uint32_t* colour, float* depth, void* stream) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    if (!r->have_frame) return fail(GBR_ERR_INVALID_ARG, "no frame rendered");
+    cudaStream_t s = (cudaStream_t)stream;
+    gbr_status st = finish_frame(r, s);
+    if (st != GBR_OK) return st;
+    const size_t npx = (size_t)r->W * r->H;
+    if (colour) GBR_CUDA(cudaMemcpyAsync(colour, r->d_colour, npx * 4u, cudaMemcpyDeviceToHost, s));
+    if (depth) GBR_CUDA(cudaMemcpyAsync(depth, r->d_depth, npx * 4u, cudaMemcpyDeviceToHost, s));
+    GBR_CUDA(cudaStreamSynchronize(s));
+    return GBR_OK;
+}
+
+gbr_status gbr_readback_ids(gbr_renderer* r, uint32_t* ids, void* stream) {
+    if (!r || !ids) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    if (!r->have_frame) return fail(GBR_ERR_INVALID_ARG, "no frame rendered");
+    cudaStream_t s = (cudaStream_t)stream;
+    gbr_status st = finish_frame(r, s);
+    if (st != GBR_OK) return st;
+    GBR_CUDA(cudaMemcpyAsync(ids, r->d_ids, (size_t)r->W * r->H * 4u, cudaMemcpyDeviceToHost, s));
+    GBR_CUDA(cudaStreamSynchronize(s));
+    return GBR_OK;
+}
+
+gbr_status gbr_device_buffers(gbr_renderer* r, void** d_colour, void** d_depth) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    if (d_colour) *d_colour = r->d_colour;
+    if (d_depth) *d_depth = r->d_depth;
+    return GBR_OK;
+}
+
+gbr_status gbr_get_bins(gbr_renderer* r, uint32_t* offsets, uint32_t* ids, uint64_t capacity, uint64_t* num_pairs,
+                        void* stream) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    if (!r->have_frame) return fail(GBR_ERR_INVALID_ARG, "no frame rendered");
+    cudaStream_t s = (cudaStream_t)stream;
+    gbr_status st = finish_frame(r, s);
+    if (st != GBR_OK) return st;
+    const uint32_t nb = r->nbx * r->nby;
+    std::vector<uint32_t> off(nb + 1u);
+    GBR_CUDA(cudaMemcpy(off.data(), r->d_offsets, (nb + 1u) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    const uint64_t total = off[nb];
+    if (num_pairs) *num_pairs = total;
+    if (offsets) memcpy(offsets, off.data(), (nb + 1u) * sizeof(uint32_t));
+    if (ids) {
+        if (capacity < total) return fail(GBR_ERR_INVALID_ARG, "ids capacity %llu < %llu pairs",
+                                          (unsigned long long)capacity, (unsigned long long)total);
+        if (total) GBR_CUDA(cudaMemcpy(ids, r->d_list, total * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < total; ++i) ids[i] &= ~kNoRasterBit;
+    }
+    return GBR_OK;
+}
+
+gbr_status gbr_get_stats(gbr_renderer* r, gbr_stats* out, void* stream) {
+    if (!r || !out) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    memset(out, 0, sizeof *out);
+    for (const MeshHost& m : r->meshes) out->num_triangles += m.num_tris;
+    out->overflow_reruns = r->overflow_reruns;
+    if (!r->have_frame) return GBR_OK;
+    gbr_status st = finish_frame(r, (cudaStream_t)stream);
+    if (st != GBR_OK) return st;
+    out->num_visible = r->h_ctl->num_visible;
+    out->num_pairs = r->h_ctl->num_pairs;
+    out->num_work_items = r->h_ctl->num_items;
+    out->num_float_path = r->h_ctl->num_float_path;
+    out->predicted_overflow = r->h_ctl->pred_overflow;
+    out->predicted_capacity = r->h_ctl->pred_capacity;
+    if (r->timing && r->ev_recorded) {
+        cudaEventElapsedTime(&out->ms_setup, r->ev[0], r->ev[1]);
+        cudaEventElapsedTime(&out->ms_bin, r->ev[1], r->ev[2]);
+        cudaEventElapsedTime(&out->ms_raster, r->ev[2], r->ev[3]);
+        cudaEventElapsedTime(&out->ms_total, r->ev[0], r->ev[3]);
+    }
+    return GBR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,290 @@
+// gbr_device.cuh -- device-side data layout and per-primitive math of the
+// GB300 frame hot path.
+//
+// Float discipline: the library is compiled with -fmad=false, and every fused
+// multiply-add is written as __fmaf_rn.  The fusions follow the ones nvcc
+// forms in the reference (CustomCUDARasterizer/CUDAROPs.cu,
+// CUDATextureSampler.cuh, Matrix4.h, Vector3.h): a*b + c*d -> fma(a, b, c*d),
+// s + a*b -> fma(a, b, s), a*b - c*d -> fma(a, b, -(c*d)).  Culling, bin
+// rectangles and texel addresses then round exactly as the reference does.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbr {
+
+constexpr uint32_t kInvalidPrim = 0xFFFFFFFFu;
+constexpr uint32_t kNoRasterBit = 0x80000000u;   // bin-list entry that cannot cover a pixel
+constexpr unsigned long long kEmptyVis = 0xFFFFFFFFFFFFFFFFull;
+constexpr int kFxBits = 16;                       // 16.16 fixed-point screen coordinates
+constexpr float kGuardPx = 8192.0f;               // |coord| below this: exact int64 edge functions
+constexpr uint32_t kFlagRaster = 1u;              // fixed path, covered winding, area > 0
+constexpr uint32_t kFlagFloat = 2u;               // outside the guard band: float edge functions
+constexpr int kMaxBinDim = 64;
+constexpr int kRasterThreads = 256;
+constexpr int kBatch = 256;
+
+enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
+
+struct TexDev {
+    const uint32_t* px;
+    uint32_t w, h;
+};
+
+// One mesh of the frame (CUDAMesh, CustomCUDARasterizer/CUDAMesh.h:27-65)
+// with the matrices Render() uploads to constant memory
+// (CUDARenderer.cu:237-247): WVP = Proj * View * World, World.
+struct MeshDev {
+    const void* vertices;
+    const uint32_t* indices;   // null: non-indexed list
+    uint32_t vertex_format;
+    uint32_t topology;
+    uint32_t num_vertices;
+    uint32_t num_tris;
+    uint32_t prim_base;
+    uint32_t pad[3];
+    float wvp[16];
+    float world[16];
+    TexDev tex[4];
+};
+
+// Raster setup record, 48 B: the triangle's 16.16 snapped screen vertices
+// (float bits when kFlagFloat), NDC z per vertex, 1/area, flags, mesh.
+struct __align__(16) TriSetup {
+    int x0, y0, x1, y1;
+    int x2, y2;
+    float z0, z1;
+    float z2, inv_area;
+    uint32_t flags;
+    uint32_t mesh;
+};
+static_assert(sizeof(TriSetup) == 48, "setup record is 48 bytes");
+
+// Device-side control block of one frame.
+struct Ctl {
+    unsigned long long num_pairs;
+    uint32_t num_visible;
+    uint32_t num_float_path;
+    uint32_t num_items;
+    uint32_t item_next;
+    uint32_t overflow;         // bin storage too small: the frame was not rasterised
+    uint32_t pred_overflow;    // a predicted per-bin capacity was exceeded
+    unsigned long long pred_capacity;
+    uint32_t error;            // non-zero: a bounded wait gave up
+    uint32_t pad[5];
+};
+
+// Everything a kernel of the frame needs, passed by value.
+struct FrameDev {
+    uint32_t width, height;
+    uint32_t nbx, nby, bw, bh, num_bins;
+    uint32_t cull, sample, vis, clear_colour32;
+    uint32_t num_meshes, num_tris;
+    uint32_t chunk;
+    float cam_pos[3];
+    float cam_fwd[3];
+    const MeshDev* meshes;
+    TriSetup* setup;
+    uint2* rects;
+    uint32_t* counts;
+    uint32_t* offsets;        // num_bins + 1
+    uint32_t* cursors;
+    uint32_t* capacity;       // predicted per-bin capacity (predicted binning)
+    uint32_t* bin_done;
+    uint4* items;
+    uint32_t items_cap;
+    uint32_t* list;
+    unsigned long long list_cap;
+    uint32_t* colour;
+    float* depth;
+    uint32_t* ids;
+    unsigned long long* gvis;
+    Ctl* ctl;
+};
+
+// ---------------------------------------------------------------------------
+// Conversions with the semantics of nvcc's cvt.rzi (saturating, NaN -> 0),
+// written out so that the result does not depend on how a cast is lowered.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cvt_s32(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (int)0x80000000u;
+    return __float2int_rz(x);
+}
+
+__device__ __forceinline__ int cvt_s16(float x) {
+    if (x != x) return 0;
+    if (x >= 32767.0f) return 32767;
+    if (x <= -32768.0f) return -32768;
+    return __float2int_rz(x);
+}
+
+__device__ __forceinline__ uint32_t cvt_u8(float x) {
+    if (!(x > 0.0f)) return 0u;
+    if (x >= 255.0f) return 255u;
+    return (uint32_t)__float2int_rz(x);
+}
+
+__device__ __forceinline__ float M4(const float* m, int r, int c) { return m[c * 4 + r]; }
+
+struct F3 { float x, y, z; };
+
+__device__ __forceinline__ F3 f3(float x, float y, float z) { F3 o; o.x = x; o.y = y; o.z = z; return o; }
+__device__ __forceinline__ F3 sub3(F3 a, F3 b) { return f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+__device__ __forceinline__ float dot3(F3 a, F3 b) { return __fmaf_rn(a.z, b.z, __fmaf_rn(a.x, b.x, __fmul_rn(a.y, b.y))); }
+__device__ __forceinline__ F3 cross3(F3 a, F3 b) {
+    return f3(__fmaf_rn(a.y, b.z, -__fmul_rn(a.z, b.y)),
+              __fmaf_rn(a.z, b.x, -__fmul_rn(a.x, b.z)),
+              __fmaf_rn(a.x, b.y, -__fmul_rn(a.y, b.x)));
+}
+// Normalize (Vector.h:41-56): zero vector for zero magnitude.
+__device__ __forceinline__ F3 normalize3(F3 v) {
+    const float m = __fsqrt_rn(dot3(v, v));
+    if (m == 0.0f) return f3(0.f, 0.f, 0.f);
+    const float inv = __fdiv_rn(1.0f, m);
+    return f3(__fmul_rn(v.x, inv), __fmul_rn(v.y, inv), __fmul_rn(v.z, inv));
+}
+
+// Matrix<4,4> * Point4(p, 1) (Matrix4.h:158-166) as fused in GetNDCVertex.
+__device__ __forceinline__ float4 xform_point(const float* m, float px, float py, float pz) {
+    float4 o;
+    o.x = __fadd_rn(__fmaf_rn(M4(m, 0, 2), pz, __fmaf_rn(M4(m, 0, 0), px, __fmul_rn(M4(m, 0, 1), py))), M4(m, 0, 3));
+    o.y = __fadd_rn(__fmaf_rn(M4(m, 1, 2), pz, __fmaf_rn(M4(m, 1, 0), px, __fmul_rn(M4(m, 1, 1), py))), M4(m, 1, 3));
+    o.z = __fadd_rn(__fmaf_rn(M4(m, 2, 2), pz, __fmaf_rn(M4(m, 2, 0), px, __fmul_rn(M4(m, 2, 1), py))), M4(m, 2, 3));
+    o.w = __fadd_rn(__fmaf_rn(M4(m, 3, 2), pz, __fmaf_rn(M4(m, 3, 0), px, __fmul_rn(M4(m, 3, 1), py))), M4(m, 3, 3));
+    return o;
+}
+
+// Matrix<3,3> * Vector3 (Matrix3.h:126-133) on the upper 3x3 of a 4x4.
+__device__ __forceinline__ F3 rot3(const float* m, F3 v) {
+    return f3(__fmaf_rn(M4(m, 0, 2), v.z, __fmaf_rn(M4(m, 0, 0), v.x, __fmul_rn(M4(m, 0, 1), v.y))),
+              __fmaf_rn(M4(m, 1, 2), v.z, __fmaf_rn(M4(m, 1, 0), v.x, __fmul_rn(M4(m, 1, 1), v.y))),
+              __fmaf_rn(M4(m, 2, 2), v.z, __fmaf_rn(M4(m, 2, 0), v.x, __fmul_rn(M4(m, 2, 1), v.y))));
+}
+
+// Position of vertex vi (object space).
+__device__ __forceinline__ F3 fetch_position(const MeshDev& m, uint32_t vi) {
+    if (m.vertex_format == kVertexPos3Rgba8) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(m.vertices) + vi);
+        return f3(v.x, v.y, v.z);
+    }
+    const float* b = reinterpret_cast<const float*>(m.vertices) + 14u * (size_t)vi;
+    const float2 xy = __ldg(reinterpret_cast<const float2*>(b));
+    return f3(xy.x, xy.y, __ldg(b + 2));
+}
+
+// Triangle assembly (TA_Kernel, CUDARenderer.cu:716-753); strips use the
+// intended order (the reference's strip branch reads an uninitialised
+// triangle).
+__device__ __forceinline__ void tri_vertex_ids(const MeshDev& m, uint32_t local, uint32_t v[3]) {
+    if (!m.indices) {
+        v[0] = 3u * local; v[1] = 3u * local + 1u; v[2] = 3u * local + 2u;
+    } else if (m.topology == 0u) {
+        v[0] = __ldg(m.indices + 3u * local); v[1] = __ldg(m.indices + 3u * local + 1u);
+        v[2] = __ldg(m.indices + 3u * local + 2u);
+    } else {
+        v[0] = __ldg(m.indices + local); v[1] = __ldg(m.indices + local + 1u); v[2] = __ldg(m.indices + local + 2u);
+        if (local & 1u) { const uint32_t s = v[1]; v[1] = v[2]; v[2] = s; }
+    }
+}
+
+// NDC -> screen (NDCToScreenSpace, CUDAROPs.cu:88-97).
+__device__ __forceinline__ float2 to_screen(float x, float y, uint32_t w, uint32_t h) {
+    float2 s;
+    s.x = __fmul_rn(__fdiv_rn(__fadd_rn(x, 1.f), 2.f), (float)w);
+    s.y = __fmul_rn(__fdiv_rn(__fsub_rn(1.f, y), 2.f), (float)h);
+    return s;
+}
+
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float m = a;
+    if (b < m) m = b;
+    if (c < m) m = c;
+    return m;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float m = a;
+    if (b > m) m = b;
+    if (c > m) m = c;
+    return m;
+}
+__device__ __forceinline__ int clampi(int v, int lo, int hi) {
+    const int c = v < lo ? lo : v;
+    return c > hi ? hi : c;
+}
+
+// GetBoundingBox (CUDAROPs.cu:180-200) with short arithmetic, then the
+// TB_Kernel bin range (CUDARenderer.cu:935-942).  Returns x0,y0,x1,y1.
+__device__ __forceinline__ int4 bin_rect(float2 s0, float2 s1, float2 s2, const FrameDev& F) {
+    int xmin = (int)(short)(cvt_s16(min3f(s0.x, s1.x, s2.x)) - 1);
+    int ymin = (int)(short)(cvt_s16(min3f(s0.y, s1.y, s2.y)) - 1);
+    int xmax = (int)(short)(cvt_s16(max3f(s0.x, s1.x, s2.x)) + 1);
+    int ymax = (int)(short)(cvt_s16(max3f(s0.y, s1.y, s2.y)) + 1);
+    xmin = clampi(xmin, 0, (int)(short)F.width);
+    ymin = clampi(ymin, 0, (int)(short)F.height);
+    xmax = clampi(xmax, 0, (int)(short)F.width);
+    ymax = clampi(ymax, 0, (int)(short)F.height);
+    int4 r;
+    r.x = clampi(xmin / (int)F.bw, 0, (int)F.nbx);
+    r.y = clampi(ymin / (int)F.bh, 0, (int)F.nby);
+    r.z = clampi(xmax / (int)F.bw, 0, (int)F.nbx - 1);
+    r.w = clampi(ymax / (int)F.bh, 0, (int)F.nby - 1);
+    return r;
+}
+
+// Packed bin rectangle: x = bx0 | bx1 << 16, y = by0 | by1 << 16 | noRaster << 31.
+__device__ __forceinline__ uint2 pack_rect(int4 r, bool no_raster) {
+    uint2 p;
+    p.x = (uint32_t)r.x | ((uint32_t)r.z << 16);
+    p.y = (uint32_t)r.y | ((uint32_t)r.w << 16) | (no_raster ? 0x80000000u : 0u);
+    return p;
+}
+__device__ __forceinline__ uint2 empty_rect() { return make_uint2(1u, 0u); }
+
+// Exact 16.16 edge function E(P; A, B) = (P - A) x (B - A), units 2^-32 px^2.
+__device__ __forceinline__ long long edge_fx(int px_fx, int py_fx, int ax, int ay, int dx, int dy) {
+    return (long long)(px_fx - ax) * (long long)dy - (long long)(py_fx - ay) * (long long)dx;
+}
+
+// z = w2*z2 + w0*z0 + w1*z1 in the reference's fused order (CUDAROPs.cu:341).
+__device__ __forceinline__ float interp_z(float w0, float w1, float w2, float z0, float z1, float z2) {
+    return __fmaf_rn(w2, z2, __fmaf_rn(w0, z0, __fmul_rn(w1, z1)));
+}
+
+// Fixed-point weights of a pixel; false when the pixel is not covered.
+__device__ __forceinline__ bool weights_fixed(const TriSetup& t, int x, int y, float w[3]) {
+    const int Px = x << kFxBits, Py = y << kFxBits;
+    const long long e2 = edge_fx(Px, Py, t.x0, t.y0, t.x1 - t.x0, t.y1 - t.y0);
+    const long long e0 = edge_fx(Px, Py, t.x1, t.y1, t.x2 - t.x1, t.y2 - t.y1);
+    const long long e1 = edge_fx(Px, Py, t.x2, t.y2, t.x0 - t.x2, t.y0 - t.y2);
+    if ((e0 | e1 | e2) < 0) return false;
+    w[0] = __fmul_rn(__ll2float_rn(e0), t.inv_area);
+    w[1] = __fmul_rn(__ll2float_rn(e1), t.inv_area);
+    w[2] = __fmul_rn(__ll2float_rn(e2), t.inv_area);
+    return true;
+}
+
+// Float weights as IsPixelInTriangle + normalisation (CUDAROPs.cu:120-145,
+// 334-339) for triangles outside the guard band.
+__device__ __forceinline__ bool weights_float(const TriSetup& t, float px, float py, float w[3]) {
+    const float v0x = __int_as_float(t.x0), v0y = __int_as_float(t.y0);
+    const float v1x = __int_as_float(t.x1), v1y = __int_as_float(t.y1);
+    const float v2x = __int_as_float(t.x2), v2y = __int_as_float(t.y2);
+    const float eax = __fsub_rn(v1x, v0x), eay = __fsub_rn(v1y, v0y);
+    const float ebx = __fsub_rn(v2x, v1x), eby = __fsub_rn(v2y, v1y);
+    const float ecx = __fsub_rn(v0x, v2x), ecy = __fsub_rn(v0y, v2y);
+    w[2] = __fmaf_rn(__fsub_rn(px, v0x), eay, -__fmul_rn(__fsub_rn(py, v0y), eax));
+    w[0] = __fmaf_rn(__fsub_rn(px, v1x), eby, -__fmul_rn(__fsub_rn(py, v1y), ebx));
+    w[1] = __fmaf_rn(__fsub_rn(px, v2x), ecy, -__fmul_rn(__fsub_rn(py, v2y), ecx));
+    if (!(w[0] >= 0.f && w[1] >= 0.f && w[2] >= 0.f)) return false;
+    const float ax = __fsub_rn(v0x, v1x), ay = __fsub_rn(v0y, v1y);
+    const float bx = __fsub_rn(v0x, v2x), by = __fsub_rn(v0y, v2y);
+    const float area = fabsf(__fmaf_rn(ax, by, -__fmul_rn(ay, bx)));
+    w[0] = __fdiv_rn(w[0], area);
+    w[1] = __fdiv_rn(w[1], area);
+    w[2] = __fdiv_rn(w[2], area);
+    return true;
+}
+
+}  // namespace gbr

@@ -1,0 +1,258 @@
+"""Python binding of libgbr (include/gbr.h) -- the ctypes stub a host
+application would bind, shaped like the reference's CUDARenderer
+(CustomCUDARasterizer/CUDARenderer.h:31-141):
+
+    r = Renderer(width, height)                 # CUDARenderer(windowHelper)
+    r.setup_bins(nbx, nby, bw, bh, chunk)       # SetupBins
+    tex = r.add_texture(rgba8)                  # CUDATextureManager::AddCUDATexture
+    r.load_scene(scene)                         # LoadScene
+    r.render(camera, cull, sample, vis)         # EnterValidRenderingState + Render
+    colour, depth = r.readback()                # Present (headless)
+
+There is no CPU fallback: constructing a Renderer without the CUDA library
+or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgbr.so")
+
+GBR_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "OVERFLOW_RERUN", 4: "TIMEOUT",
+                5: "OUT_OF_MEMORY", 6: "NOT_FOUND"}
+BINNING_EXACT, BINNING_PREDICTED = 0, 1
+
+EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "gbr_mesh_update_vertices",
+            "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
+            "gbr_texture_upload", "gbr_texture_remove", "gbr_set_binning", "gbr_set_bin_capacity",
+            "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
+            "gbr_get_bins", "gbr_get_stats", "gbr_last_error_string", "gbr_version"]
+
+
+class GbrError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"gbr status {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("fwd", C.c_float * 3), ("view", C.c_float * 16), ("proj", C.c_float * 16)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint64), ("num_visible", C.c_uint64), ("num_pairs", C.c_uint64),
+                ("num_work_items", C.c_uint64), ("num_float_path", C.c_uint64),
+                ("overflow_reruns", C.c_uint32), ("predicted_overflow", C.c_uint32),
+                ("predicted_capacity", C.c_uint64),
+                ("ms_setup", C.c_float), ("ms_bin", C.c_float), ("ms_raster", C.c_float), ("ms_total", C.c_float)]
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def lib():
+    """Load libgbr.so (built by build.py); raises if it is missing."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing: build it with custom-gpgpu-rasterizer_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, i32, u64 = C.c_void_p, C.c_uint32, C.c_int32, C.c_uint64
+        sig = {
+            "gbr_create": [u32, u32, C.POINTER(vp)],
+            "gbr_destroy": [vp],
+            "gbr_setup_bins": [vp, u32, u32, u32, u32, u32],
+            "gbr_mesh_upload": [vp, vp, u32, u32, vp, u32, u32, vp, vp, C.POINTER(u32)],
+            "gbr_mesh_update_vertices": [vp, u32, vp, u32, vp],
+            "gbr_mesh_bind_device": [vp, vp, u32, u32, vp, u32, u32, vp, vp, C.POINTER(u32)],
+            "gbr_mesh_set_world": [vp, u32, vp],
+            "gbr_mesh_set_textures": [vp, u32, vp],
+            "gbr_scene_clear": [vp],
+            "gbr_texture_upload": [vp, vp, u32, u32, C.POINTER(i32)],
+            "gbr_texture_remove": [vp, i32],
+            "gbr_set_binning": [vp, u32],
+            "gbr_set_bin_capacity": [vp, vp, C.c_int, vp],
+            "gbr_set_timing": [vp, C.c_int],
+            "gbr_render": [vp, C.POINTER(Camera), u32, u32, u32, vp],
+            "gbr_readback": [vp, vp, vp, vp],
+            "gbr_readback_ids": [vp, vp, vp],
+            "gbr_device_buffers": [vp, C.POINTER(vp), C.POINTER(vp)],
+            "gbr_get_bins": [vp, vp, vp, u64, C.POINTER(u64), vp],
+            "gbr_get_stats": [vp, C.POINTER(Stats), vp],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        L.gbr_last_error_string.restype = C.c_char_p
+        L.gbr_last_error_string.argtypes = []
+        L.gbr_version.restype = C.c_uint32
+        L.gbr_version.argtypes = []
+        _LIB = L
+    return _LIB
+
+
+def check(status: int):
+    if status != GBR_OK:
+        raise GbrError(status, lib().gbr_last_error_string().decode(errors="replace"))
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f16(m) -> C.Array:
+    return (C.c_float * 16)(*[float(x) for x in np.asarray(m, np.float32).reshape(16)])
+
+
+def make_camera(cam) -> Camera:
+    c = Camera()
+    c.pos[:] = [float(x) for x in cam.pos]
+    c.fwd[:] = [float(x) for x in cam.fwd]
+    c.view[:] = [float(x) for x in cam.view]
+    c.proj[:] = [float(x) for x in cam.proj]
+    return c
+
+
+class Renderer:
+    """Headless CUDARenderer on the current CUDA device."""
+
+    def __init__(self, width: int, height: int):
+        self._lib = lib()
+        h = C.c_void_p()
+        check(self._lib.gbr_create(width, height, C.byref(h)))
+        self.h = h
+        self.width, self.height = width, height
+        self.nbx = self.nby = 0
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self._lib.gbr_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- setup ---------------------------------------------------------
+    def setup_bins(self, nbx: int, nby: int, bw: int, bh: int, chunk: int = 256):
+        check(self._lib.gbr_setup_bins(self.h, nbx, nby, bw, bh, chunk))
+        self.nbx, self.nby = nbx, nby
+
+    def add_texture(self, rgba8: np.ndarray) -> int:
+        t = np.ascontiguousarray(rgba8, np.uint32)
+        tid = C.c_int32()
+        check(self._lib.gbr_texture_upload(self.h, _ptr(t), t.shape[1], t.shape[0], C.byref(tid)))
+        return tid.value
+
+    def remove_texture(self, tid: int):
+        check(self._lib.gbr_texture_remove(self.h, tid))
+
+    def add_mesh(self, vertices: np.ndarray, vertex_format: int, indices=None, topology: int = 0,
+                 world=None, tex_ids=(-1, -1, -1, -1)) -> int:
+        v = np.ascontiguousarray(vertices)
+        ix = None if indices is None else np.ascontiguousarray(indices, np.uint32)
+        w = _f16(np.eye(4, dtype=np.float32) if world is None else world)
+        ids = (C.c_int32 * 4)(*tex_ids)
+        mid = C.c_uint32()
+        check(self._lib.gbr_mesh_upload(self.h, _ptr(v), len(v), vertex_format, _ptr(ix),
+                                        0 if ix is None else len(ix), topology, w, ids, C.byref(mid)))
+        return mid.value
+
+    def bind_mesh_device(self, d_vertices: int, num_vertices: int, vertex_format: int, d_indices: int = 0,
+                         num_indices: int = 0, topology: int = 0, world=None, tex_ids=(-1, -1, -1, -1)) -> int:
+        w = _f16(np.eye(4, dtype=np.float32) if world is None else world)
+        ids = (C.c_int32 * 4)(*tex_ids)
+        mid = C.c_uint32()
+        check(self._lib.gbr_mesh_bind_device(self.h, C.c_void_p(d_vertices), num_vertices, vertex_format,
+                                             C.c_void_p(d_indices) if d_indices else None, num_indices, topology,
+                                             w, ids, C.byref(mid)))
+        return mid.value
+
+    def update_vertices(self, mesh_id: int, host_ptr: int, num_vertices: int, stream: int = 0):
+        check(self._lib.gbr_mesh_update_vertices(self.h, mesh_id, C.c_void_p(host_ptr), num_vertices,
+                                                 C.c_void_p(stream) if stream else None))
+
+    def clear_scene(self):
+        check(self._lib.gbr_scene_clear(self.h))
+
+    def load_scene(self, scene, chunk: int = 256):
+        """LoadScene: bins from the scene, textures, meshes."""
+        self.setup_bins(scene.num_bins_x, scene.num_bins_y, scene.bin_w, scene.bin_h, chunk)
+        self.clear_scene()
+        self.scene = scene
+        for m in scene.meshes:
+            tex_ids = [self.add_texture(t) if t is not None else -1 for t in m.textures]
+            self.add_mesh(m.vertices, m.vertex_format, m.indices, m.topology, m.world, tex_ids)
+
+    def set_binning(self, method: int):
+        check(self._lib.gbr_set_binning(self.h, method))
+
+    def set_timing(self, on: bool):
+        check(self._lib.gbr_set_timing(self.h, 1 if on else 0))
+
+    # -- frame ---------------------------------------------------------
+    def render(self, camera, cull: int, sample: int, vis: int, stream: int = 0):
+        cam = camera if isinstance(camera, Camera) else make_camera(camera)
+        check(self._lib.gbr_render(self.h, C.byref(cam), cull, sample, vis, C.c_void_p(stream) if stream else None))
+
+    def render_scene(self, scene, stream: int = 0):
+        self.render(scene.camera, scene.cull, scene.sample, scene.vis, stream)
+
+    def readback(self, colour: Optional[np.ndarray] = None, depth: Optional[np.ndarray] = None, stream: int = 0,
+                 want_depth: bool = True):
+        n = self.width * self.height
+        colour = np.empty(n, np.uint32) if colour is None else colour
+        if want_depth and depth is None:
+            depth = np.empty(n, np.float32)
+        check(self._lib.gbr_readback(self.h, _ptr(colour), _ptr(depth) if want_depth else None,
+                                     C.c_void_p(stream) if stream else None))
+        c = colour.reshape(self.height, self.width)
+        return (c, depth.reshape(self.height, self.width)) if want_depth else (c, None)
+
+    def readback_ids(self, stream: int = 0) -> np.ndarray:
+        ids = np.empty(self.width * self.height, np.uint32)
+        check(self._lib.gbr_readback_ids(self.h, _ptr(ids), C.c_void_p(stream) if stream else None))
+        return ids.reshape(self.height, self.width)
+
+    def device_buffers(self):
+        c, d = C.c_void_p(), C.c_void_p()
+        check(self._lib.gbr_device_buffers(self.h, C.byref(c), C.byref(d)))
+        return c.value, d.value
+
+    def get_bins(self, stream: int = 0):
+        """(offsets[num_bins+1], ids) of the last frame; ids sorted within each bin."""
+        nb = self.nbx * self.nby
+        offsets = np.empty(nb + 1, np.uint32)
+        n = C.c_uint64()
+        s = C.c_void_p(stream) if stream else None
+        check(self._lib.gbr_get_bins(self.h, _ptr(offsets), None, 0, C.byref(n), s))
+        ids = np.empty(max(n.value, 1), np.uint32)
+        check(self._lib.gbr_get_bins(self.h, _ptr(offsets), _ptr(ids), n.value, C.byref(n), s))
+        ids = ids[: n.value]
+        bin_of = np.repeat(np.arange(nb, dtype=np.uint32), np.diff(offsets.astype(np.int64)))
+        return offsets, ids[np.lexsort((ids, bin_of))]
+
+    def stats(self, stream: int = 0) -> dict:
+        st = Stats()
+        check(self._lib.gbr_get_stats(self.h, C.byref(st), C.c_void_p(stream) if stream else None))
+        return {k: getattr(st, k) for k, _ in Stats._fields_}

@@ -1,0 +1,245 @@
+"""Seeded synthetic scenes for the frame hot path.
+
+No asset files or datasets are read: every workload is generated here from a
+seed.  Vertices use the reference's IVertex layout (56 B: p3 uv2 n3 tan3 c3,
+CustomCUDARasterizer/Vertex.h:113-145) or the compact soup layout (16 B:
+p3 float + RGBA8).  Matrices are column-major, element (r, c) at [c*4 + r]
+(CustomCUDARasterizer/Matrix.h:9-21).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Optional
+
+import numpy as np
+
+IVERTEX56 = np.dtype([("p", "<f4", 3), ("uv", "<f4", 2), ("n", "<f4", 3),
+                      ("tan", "<f4", 3), ("c", "<f4", 3)])
+POS3_RGBA8 = np.dtype([("p", "<f4", 3), ("rgba", "<u4")])
+assert IVERTEX56.itemsize == 56 and POS3_RGBA8.itemsize == 16
+
+VERTEX_IVERTEX56 = 0
+VERTEX_POS3_RGBA8 = 1
+
+CULL_BACKFACE, CULL_FRONTFACE, CULL_NONE = 0, 1, 2
+SAMPLE_POINT, SAMPLE_LINEAR = 0, 1
+VIS_PBR, VIS_DEPTH, VIS_NORMAL = 0, 1, 2
+TOPOLOGY_LIST, TOPOLOGY_STRIP = 0, 1
+
+CLEAR_COLOUR32 = 0x003F3F3F  # RGBA{RGBColor{0.25,0.25,0.25}} (CUDARenderer.h:135, RGBRaw.h:24-32)
+
+
+def identity16() -> np.ndarray:
+    return np.eye(4, dtype=np.float32).reshape(16)
+
+
+@dataclasses.dataclass
+class Mesh:
+    vertices: np.ndarray                  # structured, IVERTEX56 or POS3_RGBA8
+    indices: Optional[np.ndarray] = None  # uint32, None: non-indexed list
+    topology: int = TOPOLOGY_LIST
+    world: np.ndarray = dataclasses.field(default_factory=identity16)
+    textures: List[Optional[np.ndarray]] = dataclasses.field(default_factory=lambda: [None] * 4)
+
+    @property
+    def vertex_format(self) -> int:
+        return VERTEX_IVERTEX56 if self.vertices.dtype == IVERTEX56 else VERTEX_POS3_RGBA8
+
+    @property
+    def num_triangles(self) -> int:
+        if self.indices is None:
+            return len(self.vertices) // 3
+        if self.topology == TOPOLOGY_LIST:
+            return len(self.indices) // 3
+        return max(len(self.indices) - 2, 0)
+
+
+@dataclasses.dataclass
+class Camera:
+    pos: np.ndarray   # (3,) f32
+    fwd: np.ndarray   # (3,) f32
+    view: np.ndarray  # (16,) f32
+    proj: np.ndarray  # (16,) f32
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    width: int
+    height: int
+    bin_w: int
+    bin_h: int
+    camera: Camera
+    meshes: List[Mesh]
+    cull: int = CULL_BACKFACE
+    sample: int = SAMPLE_POINT
+    vis: int = VIS_PBR
+    seed: int = 0
+
+    @property
+    def num_bins_x(self) -> int:
+        return (self.width + self.bin_w - 1) // self.bin_w
+
+    @property
+    def num_bins_y(self) -> int:
+        return (self.height + self.bin_h - 1) // self.bin_h
+
+    @property
+    def num_triangles(self) -> int:
+        return sum(m.num_triangles for m in self.meshes)
+
+
+def identity_camera() -> Camera:
+    """w == 1 everywhere: NDC positions pass through the vertex stage exactly."""
+    return Camera(np.zeros(3, np.float32), np.array([0, 0, 1], np.float32), identity16(), identity16())
+
+
+def _inverse_translation(pos: np.ndarray) -> np.ndarray:
+    # Inverse of the look-at matrix of an un-rotated camera (Camera.h:26):
+    # for a pure translation the FGED1 inverse (Matrix4.h:329-361) is exact.
+    v = identity16()
+    v[12:15] = -pos.astype(np.float32)
+    return v
+
+
+def perspective_camera(pos, fov_deg: float, width: int, height: int,
+                       near: float = 0.1, far: float = 100.0) -> Camera:
+    """Camera as CustomCUDARasterizer/Camera.cpp:6-36, 97-108 builds it: looks
+    down -z, forward vector (0,0,1), projection with data[3][3] left at 1 from
+    the identity it starts from."""
+    f32 = np.float32
+    pos = np.asarray(pos, np.float32)
+    radians = f32(fov_deg) * (f32(math.pi) / f32(180.0))
+    fov = f32(math.tan(radians / f32(2.0)))
+    aspect = f32(width) / f32(height)
+    A = f32(far) / (f32(near) - f32(far))
+    B = (f32(far) * f32(near)) / (f32(near) - f32(far))
+    proj = identity16()
+    proj[0] = f32(1.0) / (aspect * fov)
+    proj[5] = f32(1.0) / fov
+    proj[10] = A
+    proj[11] = f32(-1.0)
+    proj[14] = B
+    return Camera(pos, np.array([0, 0, 1], np.float32), _inverse_translation(pos), proj)
+
+
+def checker_texture(size: int = 512, cells: int = 8, c0=(230, 230, 230), c1=(40, 60, 160)) -> np.ndarray:
+    y, x = np.mgrid[0:size, 0:size]
+    cell = size // cells
+    odd = ((x // cell) + (y // cell)) & 1
+    rgb = np.where(odd[..., None] == 1, np.array(c1, np.uint32), np.array(c0, np.uint32))
+    return (rgb[..., 0] | (rgb[..., 1] << 8) | (rgb[..., 2] << 16) | (255 << 24)).astype(np.uint32)
+
+
+def flat_texture(size: int, rgb) -> np.ndarray:
+    v = rgb[0] | (rgb[1] << 8) | (rgb[2] << 16) | (255 << 24)
+    return np.full((size, size), v, np.uint32)
+
+
+def uv_sphere_mesh(lon: int = 64, lat: int = 32, radius: float = 1.0) -> Mesh:
+    """UV sphere with a seam column (lat+1)*(lon+1) vertices; single triangles
+    at the poles, two per quad elsewhere: 2*lon*(lat-1) triangles.  Front
+    faces are counter-clockwise seen from outside."""
+    i = np.arange(lat + 1, dtype=np.float64)[:, None]
+    j = np.arange(lon + 1, dtype=np.float64)[None, :]
+    theta = i * math.pi / lat
+    phi = j * 2.0 * math.pi / lon
+    x = np.sin(theta) * np.cos(phi)
+    y = np.cos(theta) * np.ones_like(phi)
+    z = np.sin(theta) * np.sin(phi)
+    v = np.zeros((lat + 1) * (lon + 1), IVERTEX56)
+    p = np.stack([x, y, z], -1).reshape(-1, 3)
+    v["p"] = (p * radius).astype(np.float32)
+    v["n"] = p.astype(np.float32)
+    v["uv"] = np.stack([np.broadcast_to(j / lon, x.shape), np.broadcast_to(i / lat, x.shape)], -1).reshape(-1, 2)
+    tan = np.stack([-np.sin(phi) * np.ones_like(theta), np.zeros_like(x), np.cos(phi) * np.ones_like(theta)], -1)
+    v["tan"] = tan.reshape(-1, 3).astype(np.float32)
+    v["c"] = 1.0
+    idx = []
+    vid = lambda a, b: a * (lon + 1) + b
+    for a in range(lat):
+        for b in range(lon):
+            q0, q1, q2, q3 = vid(a, b), vid(a + 1, b), vid(a + 1, b + 1), vid(a, b + 1)
+            if a != 0:
+                idx.append((q0, q1, q3))
+            if a != lat - 1:
+                idx.append((q1, q2, q3) if a != 0 else (q0, q1, q2))
+    tri = np.array(idx, np.int64)
+    pp = v["p"].astype(np.float64)
+    nrm = np.cross(pp[tri[:, 1]] - pp[tri[:, 0]], pp[tri[:, 2]] - pp[tri[:, 0]])
+    cen = pp[tri].mean(axis=1)
+    flip = (nrm * cen).sum(-1) < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    return Mesh(vertices=v, indices=tri.reshape(-1).astype(np.uint32))
+
+
+def sphere_scene(width: int = 640, height: int = 480, bin_size: int = 16, lon: int = 64, lat: int = 32,
+                 tex_size: int = 512, sample: int = SAMPLE_POINT, vis: int = VIS_PBR) -> Scene:
+    """UV sphere (64x32), r=1 at the origin, camera at distance 3 with a 60 deg
+    FOV, 512^2 checker with 8x8 cells.  Lambert + ambient shading is the
+    reference's shader with all four maps bound: checker diffuse, flat normal
+    map (128,128,255), black specular, grey gloss (ShadePixelSafe,
+    CustomCUDARasterizer/CUDAROPs.cu:411-470)."""
+    mesh = uv_sphere_mesh(lon, lat)
+    mesh.textures = [checker_texture(tex_size, 8), flat_texture(tex_size, (128, 128, 255)),
+                     flat_texture(tex_size, (0, 0, 0)), flat_texture(tex_size, (128, 128, 128))]
+    cam = perspective_camera((0.0, 0.0, 3.0), 60.0, width, height)
+    return Scene("sphere", width, height, bin_size, bin_size, cam, [mesh], cull=CULL_BACKFACE,
+                 sample=sample, vis=vis)
+
+
+def soup_vertices(n: int, width: int, height: int, seed: int = 0, blob_frac: float = 0.2,
+                  blob_sigma: float = 100.0, area_min: float = 0.5, area_max: float = 4096.0) -> np.ndarray:
+    """Triangle soup in NDC with w == 1: centroids uniform over the screen plus
+    a Gaussian blob (sigma px) at the centre, area log-uniform in
+    [area_min, area_max] px^2, random orientation and winding, depth uniform in
+    [0.1, 100] mapped to z_ndc = (d - 0.1) / 99.9, RGBA8 vertex colours."""
+    rng = np.random.default_rng(seed)
+    nb = int(round(n * blob_frac))
+    cx = np.empty(n)
+    cy = np.empty(n)
+    cx[: n - nb] = rng.uniform(0, width, n - nb)
+    cy[: n - nb] = rng.uniform(0, height, n - nb)
+    cx[n - nb:] = rng.normal(width / 2, blob_sigma, nb)
+    cy[n - nb:] = rng.normal(height / 2, blob_sigma, nb)
+    perm = rng.permutation(n)
+    cx, cy = cx[perm], cy[perm]
+    area = np.exp(rng.uniform(math.log(area_min), math.log(area_max), n))
+    base = rng.uniform(0, 2 * math.pi, n)
+    ang = base[:, None] + np.arange(3)[None, :] * (2 * math.pi / 3) + rng.uniform(-0.6, 0.6, (n, 3))
+    ux, uy = np.cos(ang), np.sin(ang)
+    unit_area = 0.5 * np.abs((ux[:, 1] - ux[:, 0]) * (uy[:, 2] - uy[:, 0]) - (uy[:, 1] - uy[:, 0]) * (ux[:, 2] - ux[:, 0]))
+    r = np.sqrt(area / np.maximum(unit_area, 1e-6))
+    px = cx[:, None] + r[:, None] * ux
+    py = cy[:, None] + r[:, None] * uy
+    flip = rng.random(n) < 0.5
+    px[flip] = px[flip][:, [0, 2, 1]]
+    py[flip] = py[flip][:, [0, 2, 1]]
+    d = rng.uniform(0.1, 100.0, n)[:, None] * (1.0 + rng.uniform(-0.01, 0.01, (n, 3)))
+    d = np.clip(d, 0.1, 100.0)
+    v = np.zeros(3 * n, POS3_RGBA8)
+    xn = (2.0 * px / width - 1.0).astype(np.float32)
+    yn = (1.0 - 2.0 * py / height).astype(np.float32)
+    zn = ((d - 0.1) / 99.9).astype(np.float32)
+    v["p"] = np.stack([xn, yn, zn], -1).reshape(-1, 3)
+    rgb = rng.integers(0, 256, (3 * n, 3), dtype=np.uint32)
+    v["rgba"] = rgb[:, 0] | (rgb[:, 1] << 8) | (rgb[:, 2] << 16) | np.uint32(255 << 24)
+    return v
+
+
+def soup_scene(n: int = 1_000_000, width: int = 1920, height: int = 1080, bin_size: int = 16, seed: int = 0,
+               cull: int = CULL_NONE, ivertex: bool = False) -> Scene:
+    v = soup_vertices(n, width, height, seed)
+    if ivertex:
+        v = pos3_to_ivertex(v)
+    return Scene(f"soup{n}", width, height, bin_size, bin_size, identity_camera(), [Mesh(vertices=v)],
+                 cull=cull, seed=seed)
+
+
+def pos3_to_ivertex(v: np.ndarray) -> np.ndarray:
+    out = np.zeros(len(v), IVERTEX56)
+    out["p"] = v["p"]
+    rgba = v["rgba"]
+    out["c"] = np.stack([(rgba & 0xFF), (rgba >> 8) & 0xFF, (rgba >> 16) & 0xFF], -1).astype(np.float32) / np.float32(255.0)
+    return out

@@ -1,0 +1,161 @@
+/*
+ * gbr.h -- C ABI of the GB300 frame-hot-path renderer.
+ *
+ * Drop-in for the per-frame path of Custom-CUDA-Rasterizer's CUDARenderer
+ * (CustomCUDARasterizer/CUDARenderer.h:31-141): mesh and texture upload
+ * (CUDAMesh, CUDATextureManager), bin setup, the per-frame render call with
+ * CullingMode / SampleState / VisualisationState, and the framebuffer
+ * readback that Present() performs.  Plain C types only; a CUDA stream is
+ * passed as void* (cudaStream_t), NULL meaning the legacy default stream.
+ *
+ * Every entry point returns a gbr_status; none exits or throws.  The message
+ * of the last failure on the calling thread is gbr_last_error_string().
+ *
+ * Enum values are the reference's integer values (CullingMode.h,
+ * VisualisationState.h, SampleState.h, PrimitiveTopology.h).
+ */
+#ifndef GBR_H
+#define GBR_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBR_OK = 0,
+    GBR_ERR_INVALID_ARG = 1,
+    GBR_ERR_CUDA = 2,
+    GBR_ERR_OVERFLOW_RERUN = 3, /* informational: a frame was re-binned after a capacity overflow */
+    GBR_ERR_TIMEOUT = 4,
+    GBR_ERR_OUT_OF_MEMORY = 5,
+    GBR_ERR_NOT_FOUND = 6
+} gbr_status;
+
+/* CullingMode (CullingMode.h:3-7) */
+enum { GBR_CULL_BACKFACE = 0, GBR_CULL_FRONTFACE = 1, GBR_CULL_NONE = 2 };
+/* SampleState (SampleState.h:3-7) */
+enum { GBR_SAMPLE_POINT = 0, GBR_SAMPLE_LINEAR = 1 };
+/* VisualisationState (VisualisationState.h:3-7) */
+enum { GBR_VIS_PBR = 0, GBR_VIS_DEPTH = 1, GBR_VIS_NORMAL = 2 };
+/* PrimitiveTopology (PrimitiveTopology.h:3-7) */
+enum { GBR_TOPOLOGY_TRIANGLE_LIST = 0, GBR_TOPOLOGY_TRIANGLE_STRIP = 1 };
+/* Vertex layouts accepted by gbr_mesh_upload */
+enum {
+    GBR_VERTEX_IVERTEX56 = 0,  /* IVertex (Vertex.h:113-145): p3 uv2 n3 tan3 c3 floats, 56 B */
+    GBR_VERTEX_POS3_RGBA8 = 1  /* p3 floats + RGBA8 colour (byte0 = R), 16 B */
+};
+/* Texture slots (Mesh::TextureID, Mesh.h:9-15) */
+enum { GBR_TEX_DIFFUSE = 0, GBR_TEX_NORMAL = 1, GBR_TEX_SPECULAR = 2, GBR_TEX_GLOSSINESS = 3 };
+/* Binning method */
+enum { GBR_BINNING_EXACT = 0, GBR_BINNING_PREDICTED = 1 };
+
+typedef struct gbr_renderer gbr_renderer;
+
+/* Camera state Render() reads (CUDARenderer.cu:215-219): position, forward
+ * (the look-at matrix's third column), view and projection matrices, column
+ * major with element (r, c) at [c*4 + r] (Matrix.h:9-21). */
+typedef struct {
+    float pos[3];
+    float fwd[3];
+    float view[16];
+    float proj[16];
+} gbr_camera;
+
+typedef struct {
+    uint64_t num_triangles;      /* GetTotalNumTriangles (CUDARenderer.h:64) */
+    uint64_t num_visible;        /* GetTotalNumVisibleTriangles (CUDARenderer.h:63) */
+    uint64_t num_pairs;          /* (triangle, bin) pairs of the last frame */
+    uint64_t num_work_items;     /* raster work items (bin chunks) */
+    uint64_t num_float_path;     /* visible triangles outside the fixed-point guard band */
+    uint32_t overflow_reruns;    /* frames re-binned exactly after a capacity overflow */
+    uint32_t predicted_overflow; /* last predicted-capacity frame overflowed a bin */
+    uint64_t predicted_capacity; /* sum of predicted per-bin capacities, last frame */
+    float ms_setup, ms_bin, ms_raster, ms_total; /* per-stage times of the last frame with timing on */
+} gbr_stats;
+
+/* CUDARenderer(const WindowHelper&) (CUDARenderer.cu:33-46): headless, the
+ * frame buffers live on the current CUDA device. */
+gbr_status gbr_create(uint32_t width, uint32_t height, gbr_renderer **out);
+/* ~CUDARenderer (CUDARenderer.cu:48-53) */
+gbr_status gbr_destroy(gbr_renderer *r);
+
+/* SetupBins(numBins, binDim, queueMaxSize) (CUDARenderer.cu:199-204).
+ * queue_chunk replaces the fixed queue capacity: bins are exact-sized, and
+ * a bin's list is rasterised in chunks of at most queue_chunk triangles. */
+gbr_status gbr_setup_bins(gbr_renderer *r, uint32_t num_bins_x, uint32_t num_bins_y,
+                          uint32_t bin_w, uint32_t bin_h, uint32_t queue_chunk);
+
+/* LoadScene -> new CUDAMesh(Mesh*) (CUDARenderer.cu:177-197, CUDAMesh.cpp:4-20,
+ * 42-59): copies the host vertex and index buffers to the device.
+ * indices may be NULL for a non-indexed triangle list (vertex 3t+k of
+ * triangle t).  world: the mesh's world matrix.  tex_ids: texture ids
+ * (-1 = none) resolved as UpdateCUDAMeshTextures (CUDARenderer.cu:542-573). */
+gbr_status gbr_mesh_upload(gbr_renderer *r, const void *vertices, uint32_t num_vertices,
+                           uint32_t vertex_format, const uint32_t *indices, uint32_t num_indices,
+                           uint32_t topology, const float world[16], const int32_t tex_ids[4],
+                           uint32_t *mesh_id);
+/* Replace a mesh's vertices (same count and layout) with an asynchronous
+ * host-to-device copy on `stream`; host memory should be pinned. */
+gbr_status gbr_mesh_update_vertices(gbr_renderer *r, uint32_t mesh_id, const void *vertices,
+                                    uint32_t num_vertices, void *stream);
+/* Bind device-resident vertices (and optional indices) that the caller owns
+ * and keeps alive; no copy is made. */
+gbr_status gbr_mesh_bind_device(gbr_renderer *r, const void *d_vertices, uint32_t num_vertices,
+                                uint32_t vertex_format, const uint32_t *d_indices, uint32_t num_indices,
+                                uint32_t topology, const float world[16], const int32_t tex_ids[4],
+                                uint32_t *mesh_id);
+/* CUDAMesh::GetWorld() assignment (CUDAMesh.h:17-18) */
+gbr_status gbr_mesh_set_world(gbr_renderer *r, uint32_t mesh_id, const float world[16]);
+gbr_status gbr_mesh_set_textures(gbr_renderer *r, uint32_t mesh_id, const int32_t tex_ids[4]);
+/* FreeAllCUDAMeshBuffers (CUDARenderer.cu:488-496) */
+gbr_status gbr_scene_clear(gbr_renderer *r);
+
+/* CUDATexture::Create + CUDATextureManager::AddCUDATexture
+ * (CUDATexture.cpp:24-72, CUDATextureManager.cpp:29-37): RGBA8 texels,
+ * byte0 = R as the sampler reads them (RGBRaw.h:34-38), rows of w texels. */
+gbr_status gbr_texture_upload(gbr_renderer *r, const uint32_t *rgba8, uint32_t w, uint32_t h, int32_t *tex_id);
+/* CUDATextureManager::RemoveCUDATexture (CUDATextureManager.cpp:39-54) */
+gbr_status gbr_texture_remove(gbr_renderer *r, int32_t tex_id);
+
+/* Binning method for the following frames. */
+gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
+/* Per-bin capacities for GBR_BINNING_PREDICTED (device or host pointer
+ * according to is_device), num_bins_x*num_bins_y entries. */
+gbr_status gbr_set_bin_capacity(gbr_renderer *r, const uint32_t *capacity, int is_device, void *stream);
+/* Record per-stage CUDA-event times into gbr_stats (off by default). */
+gbr_status gbr_set_timing(gbr_renderer *r, int enabled);
+
+/* EnterValidRenderingState + Render (CUDARenderer.cu:206-381): clears, runs
+ * the whole frame on `stream` and returns without synchronising.  The
+ * framebuffer holds RGBA::GetRGBAFromColour words (bytes B, G, R, 0). */
+gbr_status gbr_render(gbr_renderer *r, const gbr_camera *cam, uint32_t cull, uint32_t sample,
+                      uint32_t vis, void *stream);
+
+/* Present (CUDARenderer.cu:383-395) without a window: waits for `stream`
+ * and copies the framebuffer (and optionally the per-pixel interpolated
+ * depth, 0 where no fragment landed) to host memory.  If the frame's bin
+ * storage overflowed, the frame is re-rendered with exact storage first. */
+gbr_status gbr_readback(gbr_renderer *r, uint32_t *colour, float *depth, void *stream);
+/* Winning primitive id per pixel (0xFFFFFFFF where empty). */
+gbr_status gbr_readback_ids(gbr_renderer *r, uint32_t *ids, void *stream);
+/* Device addresses of the colour (uint32) and depth (float) buffers. */
+gbr_status gbr_device_buffers(gbr_renderer *r, void **d_colour, void **d_depth);
+/* Per-bin triangle lists of the last frame: offsets[num_bins+1] and
+ * ids[capacity] (global primitive ids; order inside a bin unspecified).
+ * *num_pairs gets the total; GBR_ERR_INVALID_ARG when capacity is short. */
+gbr_status gbr_get_bins(gbr_renderer *r, uint32_t *offsets, uint32_t *ids, uint64_t capacity,
+                        uint64_t *num_pairs, void *stream);
+/* GetTotalNumVisibleTriangles / GetTotalNumTriangles and per-stage timers
+ * (CUDARenderer.h:63-73); synchronises with `stream`. */
+gbr_status gbr_get_stats(gbr_renderer *r, gbr_stats *out, void *stream);
+
+const char *gbr_last_error_string(void);
+/* Library version, e.g. 0x000100 for 0.1.0. */
+uint32_t gbr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
