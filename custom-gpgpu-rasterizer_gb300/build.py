@@ -29,12 +29,14 @@ def nvcc() -> str:
 def _inputs():
     files = [os.path.join(CSRC, f) for f in SOURCES + HEADERS]
     files.append(os.path.join(ROOT, "include", "gbr.h"))
+    files.append(os.path.join(ROOT, "include", "gbr_cudarenderer.hpp"))
+    files.append(os.path.join(ROOT, "tests", "cpp", "facade_render.cpp"))
     files.append(os.path.abspath(__file__))
     return files
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(FACADE_BIN):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(f) <= t for f in _inputs())
@@ -66,7 +68,23 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     subprocess.run([nvcc(), "-shared", *ARCH, *objs, "-o", tmp, "-lcudart"], check=True)
     os.replace(tmp, LIB)
+    build_facade_demo()
     return LIB
+
+
+FACADE_SRC = os.path.join(ROOT, "tests", "cpp", "facade_render.cpp")
+FACADE_BIN = os.path.join(OUT_DIR, "facade_render")
+
+
+def build_facade_demo() -> str:
+    """Compiles the C++ host-API driver (tests/cpp/facade_render.cpp) with the
+    host compiler against include/gbr_cudarenderer.hpp and libgbr.so."""
+    if not os.path.exists(FACADE_SRC):
+        return ""
+    cxx = os.environ.get("CXX", "g++")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), FACADE_SRC,
+                    "-L", OUT_DIR, "-lgbr", "-Wl,-rpath," + OUT_DIR, "-o", FACADE_BIN], check=True)
+    return FACADE_BIN
 
 
 if __name__ == "__main__":

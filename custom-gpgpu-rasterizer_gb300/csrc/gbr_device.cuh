@@ -48,11 +48,12 @@ struct MeshDev {
     TexDev tex[4];
 };
 
-// Raster setup record, 48 B: the triangle's 16.16 snapped screen vertices
-// (float bits when kFlagFloat), NDC z per vertex, 1/area, flags, mesh.
+// Raster setup record, 48 B: the triangle's float screen vertices (the
+// raster snaps them to 16.16 for coverage), NDC z per vertex, 1 / the float
+// area the reference divides its weights by, flags, mesh index.
 struct __align__(16) TriSetup {
-    int x0, y0, x1, y1;
-    int x2, y2;
+    float x0, y0, x1, y1;
+    float x2, y2;
     float z0, z1;
     float z2, inv_area;
     uint32_t flags;
@@ -252,34 +253,37 @@ __device__ __forceinline__ float interp_z(float w0, float w1, float w2, float z0
     return __fmaf_rn(w2, z2, __fmaf_rn(w0, z0, __fmul_rn(w1, z1)));
 }
 
-// Fixed-point weights of a pixel; false when the pixel is not covered.
-__device__ __forceinline__ bool weights_fixed(const TriSetup& t, int x, int y, float w[3]) {
-    const int Px = x << kFxBits, Py = y << kFxBits;
-    const long long e2 = edge_fx(Px, Py, t.x0, t.y0, t.x1 - t.x0, t.y1 - t.y0);
-    const long long e0 = edge_fx(Px, Py, t.x1, t.y1, t.x2 - t.x1, t.y2 - t.y1);
-    const long long e1 = edge_fx(Px, Py, t.x2, t.y2, t.x0 - t.x2, t.y0 - t.y2);
-    if ((e0 | e1 | e2) < 0) return false;
-    w[0] = __fmul_rn(__ll2float_rn(e0), t.inv_area);
-    w[1] = __fmul_rn(__ll2float_rn(e1), t.inv_area);
-    w[2] = __fmul_rn(__ll2float_rn(e2), t.inv_area);
-    return true;
+__device__ __forceinline__ int snap_fx(float v) { return __float2int_rn(__fmul_rn(v, 65536.f)); }
+
+// The reference's float edge functions at a pixel (IsPixelInTriangle,
+// CUDAROPs.cu:120-142): w[2] from edge v0->v1, w[0] from v1->v2, w[1] from
+// v2->v0.
+__device__ __forceinline__ void edges_ref(const TriSetup& t, float px, float py, float w[3]) {
+    const float eax = __fsub_rn(t.x1, t.x0), eay = __fsub_rn(t.y1, t.y0);
+    const float ebx = __fsub_rn(t.x2, t.x1), eby = __fsub_rn(t.y2, t.y1);
+    const float ecx = __fsub_rn(t.x0, t.x2), ecy = __fsub_rn(t.y0, t.y2);
+    w[2] = __fmaf_rn(__fsub_rn(px, t.x0), eay, -__fmul_rn(__fsub_rn(py, t.y0), eax));
+    w[0] = __fmaf_rn(__fsub_rn(px, t.x1), eby, -__fmul_rn(__fsub_rn(py, t.y1), ebx));
+    w[1] = __fmaf_rn(__fsub_rn(px, t.x2), ecy, -__fmul_rn(__fsub_rn(py, t.y2), ecx));
 }
 
-// Float weights as IsPixelInTriangle + normalisation (CUDAROPs.cu:120-145,
-// 334-339) for triangles outside the guard band.
+// Interpolation weights of a pixel covered under the fixed-point rule: the
+// reference's float edge values times 1/area (coverage itself is decided on
+// the snapped triangle by the raster).
+__device__ __forceinline__ void weights_fixed(const TriSetup& t, int x, int y, float w[3]) {
+    edges_ref(t, (float)x, (float)y, w);
+    w[0] = __fmul_rn(w[0], t.inv_area);
+    w[1] = __fmul_rn(w[1], t.inv_area);
+    w[2] = __fmul_rn(w[2], t.inv_area);
+}
+
+// Float coverage and weights as IsPixelInTriangle + normalisation
+// (CUDAROPs.cu:120-145, 334-339), for triangles outside the guard band.
 __device__ __forceinline__ bool weights_float(const TriSetup& t, float px, float py, float w[3]) {
-    const float v0x = __int_as_float(t.x0), v0y = __int_as_float(t.y0);
-    const float v1x = __int_as_float(t.x1), v1y = __int_as_float(t.y1);
-    const float v2x = __int_as_float(t.x2), v2y = __int_as_float(t.y2);
-    const float eax = __fsub_rn(v1x, v0x), eay = __fsub_rn(v1y, v0y);
-    const float ebx = __fsub_rn(v2x, v1x), eby = __fsub_rn(v2y, v1y);
-    const float ecx = __fsub_rn(v0x, v2x), ecy = __fsub_rn(v0y, v2y);
-    w[2] = __fmaf_rn(__fsub_rn(px, v0x), eay, -__fmul_rn(__fsub_rn(py, v0y), eax));
-    w[0] = __fmaf_rn(__fsub_rn(px, v1x), eby, -__fmul_rn(__fsub_rn(py, v1y), ebx));
-    w[1] = __fmaf_rn(__fsub_rn(px, v2x), ecy, -__fmul_rn(__fsub_rn(py, v2y), ecx));
+    edges_ref(t, px, py, w);
     if (!(w[0] >= 0.f && w[1] >= 0.f && w[2] >= 0.f)) return false;
-    const float ax = __fsub_rn(v0x, v1x), ay = __fsub_rn(v0y, v1y);
-    const float bx = __fsub_rn(v0x, v2x), by = __fsub_rn(v0y, v2y);
+    const float ax = __fsub_rn(t.x0, t.x1), ay = __fsub_rn(t.y0, t.y1);
+    const float bx = __fsub_rn(t.x0, t.x2), by = __fsub_rn(t.y0, t.y2);
     const float area = fabsf(__fmaf_rn(ax, by, -__fmul_rn(ay, bx)));
     w[0] = __fdiv_rn(w[0], area);
     w[1] = __fdiv_rn(w[1], area);

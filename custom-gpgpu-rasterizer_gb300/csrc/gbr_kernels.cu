@@ -110,35 +110,32 @@ __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
             const float2 s1 = to_screen(nx[1], ny[1], F.width, F.height);
             const float2 s2 = to_screen(nx[2], ny[2], F.width, F.height);
             const int4 r = bin_rect(s0, s1, s2, F);
-            TriSetup t;
-            t.z0 = nz[0]; t.z1 = nz[1]; t.z2 = nz[2];
-            t.mesh = mi;
             const bool inside = fabsf(s0.x) < kGuardPx && fabsf(s0.y) < kGuardPx && fabsf(s1.x) < kGuardPx &&
                                 fabsf(s1.y) < kGuardPx && fabsf(s2.x) < kGuardPx && fabsf(s2.y) < kGuardPx;
+            float inv_area = 0.f;
+            uint32_t flags;
             if (inside) {
-                t.x0 = __float2int_rn(__fmul_rn(s0.x, 65536.f)); t.y0 = __float2int_rn(__fmul_rn(s0.y, 65536.f));
-                t.x1 = __float2int_rn(__fmul_rn(s1.x, 65536.f)); t.y1 = __float2int_rn(__fmul_rn(s1.y, 65536.f));
-                t.x2 = __float2int_rn(__fmul_rn(s2.x, 65536.f)); t.y2 = __float2int_rn(__fmul_rn(s2.y, 65536.f));
-                // S = cross(v0 - v1, v2 - v1) > 0 <=> the covered winding; S = 2*area
-                const long long S = (long long)(t.x0 - t.x1) * (long long)(t.y2 - t.y1) -
-                                    (long long)(t.y0 - t.y1) * (long long)(t.x2 - t.x1);
-                no_raster = S <= 0;
-                t.inv_area = no_raster ? 0.f : __fdiv_rn(1.0f, __ll2float_rn(S));
-                t.flags = no_raster ? 0u : kFlagRaster;
+                const int X0 = snap_fx(s0.x), Y0 = snap_fx(s0.y), X1 = snap_fx(s1.x);
+                const int Y1 = snap_fx(s1.y), X2 = snap_fx(s2.x), Y2 = snap_fx(s2.y);
+                // S = cross(v0 - v1, v2 - v1) of the snapped triangle: > 0 for the
+                // covered winding (the three edge functions sum to S)
+                const long long S = (long long)(X0 - X1) * (long long)(Y2 - Y1) -
+                                    (long long)(Y0 - Y1) * (long long)(X2 - X1);
+                // the float area the reference divides its weights by (CUDAROPs.cu:336)
+                const float area = fabsf(__fmaf_rn(__fsub_rn(s0.x, s1.x), __fsub_rn(s0.y, s2.y),
+                                                   -__fmul_rn(__fsub_rn(s0.y, s1.y), __fsub_rn(s0.x, s2.x))));
+                no_raster = !(S > 0 && area > 0.f);
+                inv_area = no_raster ? 0.f : __fdiv_rn(1.0f, area);
+                flags = no_raster ? 0u : kFlagRaster;
             } else {
                 fpath = true;
                 no_raster = false;
-                t.x0 = __float_as_int(s0.x); t.y0 = __float_as_int(s0.y);
-                t.x1 = __float_as_int(s1.x); t.y1 = __float_as_int(s1.y);
-                t.x2 = __float_as_int(s2.x); t.y2 = __float_as_int(s2.y);
-                t.inv_area = 0.f;
-                t.flags = kFlagFloat;
+                flags = kFlagFloat;
             }
-            reinterpret_cast<uint4*>(F.setup)[3u * prim] = make_uint4(t.x0, t.y0, t.x1, t.y1);
-            reinterpret_cast<uint4*>(F.setup)[3u * prim + 1u] =
-                make_uint4(t.x2, t.y2, __float_as_uint(t.z0), __float_as_uint(t.z1));
-            reinterpret_cast<uint4*>(F.setup)[3u * prim + 2u] =
-                make_uint4(__float_as_uint(t.z2), __float_as_uint(t.inv_area), t.flags, t.mesh);
+            uint4* rec = reinterpret_cast<uint4*>(F.setup) + 3u * prim;
+            rec[0] = make_uint4(__float_as_uint(s0.x), __float_as_uint(s0.y), __float_as_uint(s1.x), __float_as_uint(s1.y));
+            rec[1] = make_uint4(__float_as_uint(s2.x), __float_as_uint(s2.y), __float_as_uint(nz[0]), __float_as_uint(nz[1]));
+            rec[2] = make_uint4(__float_as_uint(nz[2]), __float_as_uint(inv_area), flags, mi);
             rect = pack_rect(r, no_raster);
         }
         F.rects[prim] = rect;
@@ -242,8 +239,10 @@ struct RasterShared {
 
 __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
                                              int ty0, int tw, int th, uint32_t lane) {
-    const int minx = min(t.x0, min(t.x1, t.x2)), maxx = max(t.x0, max(t.x1, t.x2));
-    const int miny = min(t.y0, min(t.y1, t.y2)), maxy = max(t.y0, max(t.y1, t.y2));
+    const int X0 = snap_fx(t.x0), Y0 = snap_fx(t.y0), X1 = snap_fx(t.x1);
+    const int Y1 = snap_fx(t.y1), X2 = snap_fx(t.x2), Y2 = snap_fx(t.y2);
+    const int minx = min(X0, min(X1, X2)), maxx = max(X0, max(X1, X2));
+    const int miny = min(Y0, min(Y1, Y2)), maxy = max(Y0, max(Y1, Y2));
     // covered pixels lie in [ceil(min), floor(max)] of the snapped triangle
     const int px0 = max((minx + 0xFFFF) >> kFxBits, tx0), px1 = min(maxx >> kFxBits, tx0 + tw - 1);
     const int py0 = max((miny + 0xFFFF) >> kFxBits, ty0), py1 = min(maxy >> kFxBits, ty0 + th - 1);
@@ -252,23 +251,22 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
     const int lsw = bwid <= 1 ? 0 : bwid <= 2 ? 1 : bwid <= 4 ? 2 : bwid <= 8 ? 3 : bwid <= 16 ? 4 : 5;
     const int sw = 1 << lsw, sh = 32 >> lsw;
     const int lx = (int)lane & (sw - 1), ly = (int)lane >> lsw;
-    const int dxa = t.x1 - t.x0, dya = t.y1 - t.y0;
-    const int dxb = t.x2 - t.x1, dyb = t.y2 - t.y1;
-    const int dxc = t.x0 - t.x2, dyc = t.y0 - t.y2;
+    const int dxa = X1 - X0, dya = Y1 - Y0;
+    const int dxb = X2 - X1, dyb = Y2 - Y1;
+    const int dxc = X0 - X2, dyc = Y0 - Y2;
     for (int sy = py0; sy <= py1; sy += sh) {
         const int y = sy + ly;
         for (int sx = px0; sx <= px1; sx += sw) {
             const int x = sx + lx;
             if (x > px1 || y > py1) continue;
             const int Px = x << kFxBits, Py = y << kFxBits;
-            const long long e2 = edge_fx(Px, Py, t.x0, t.y0, dxa, dya);
-            const long long e0 = edge_fx(Px, Py, t.x1, t.y1, dxb, dyb);
-            const long long e1 = edge_fx(Px, Py, t.x2, t.y2, dxc, dyc);
+            const long long e2 = edge_fx(Px, Py, X0, Y0, dxa, dya);
+            const long long e0 = edge_fx(Px, Py, X1, Y1, dxb, dyb);
+            const long long e1 = edge_fx(Px, Py, X2, Y2, dxc, dyc);
             if ((e0 | e1 | e2) < 0) continue;
-            const float w0 = __fmul_rn(__ll2float_rn(e0), t.inv_area);
-            const float w1 = __fmul_rn(__ll2float_rn(e1), t.inv_area);
-            const float w2 = __fmul_rn(__ll2float_rn(e2), t.inv_area);
-            const float z = interp_z(w0, w1, w2, t.z0, t.z1, t.z2);
+            float w[3];
+            weights_fixed(t, x, y, w);
+            const float z = interp_z(w[0], w[1], w[2], t.z0, t.z1, t.z2);
             // the reference rejects z < 0 or z > 1; z == 1 saturates the key to
             // INT_MAX and can never win the depth test (CUDAROPs.cu:343-345, 386)
             if (!(z >= 0.f && z < 1.f)) continue;
@@ -283,8 +281,7 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
 // Triangles outside the guard band: the reference's float edge functions.
 __device__ __forceinline__ void raster_float(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
                                              int ty0, int tw, int th, uint32_t lane) {
-    const float x0 = __int_as_float(t.x0), y0 = __int_as_float(t.y0), x1 = __int_as_float(t.x1);
-    const float y1 = __int_as_float(t.y1), x2 = __int_as_float(t.x2), y2 = __int_as_float(t.y2);
+    const float x0 = t.x0, y0 = t.y0, x1 = t.x1, y1 = t.y1, x2 = t.x2, y2 = t.y2;
     if (x0 != x0 || y0 != y0 || x1 != x1 || y1 != y1 || x2 != x2 || y2 != y2) return;
     int px0 = tx0, px1 = tx0 + tw - 1, py0 = ty0, py1 = ty0 + th - 1;
     const float fx0 = floorf(min3f(x0, x1, x2)) - 1.f, fx1 = ceilf(max3f(x0, x1, x2)) + 1.f;
@@ -322,8 +319,8 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& F, int x, int y, u
     const uint4* rp = reinterpret_cast<const uint4*>(F.setup) + 3u * prim;
     const uint4 a = __ldg(rp), b = __ldg(rp + 1), c = __ldg(rp + 2);
     TriSetup t;
-    t.x0 = (int)a.x; t.y0 = (int)a.y; t.x1 = (int)a.z; t.y1 = (int)a.w;
-    t.x2 = (int)b.x; t.y2 = (int)b.y; t.z0 = __uint_as_float(b.z); t.z1 = __uint_as_float(b.w);
+    t.x0 = __uint_as_float(a.x); t.y0 = __uint_as_float(a.y); t.x1 = __uint_as_float(a.z); t.y1 = __uint_as_float(a.w);
+    t.x2 = __uint_as_float(b.x); t.y2 = __uint_as_float(b.y); t.z0 = __uint_as_float(b.z); t.z1 = __uint_as_float(b.w);
     t.z2 = __uint_as_float(c.x); t.inv_area = __uint_as_float(c.y); t.flags = c.z; t.mesh = c.w;
     float w[3] = {0.f, 0.f, 0.f};
     if (t.flags & kFlagFloat) weights_float(t, (float)x, (float)y, w);

@@ -364,8 +364,8 @@ typedef struct {
     v2 s[3];            /* float screen coords */
     float z[3];         /* NDC z */
     int32_t X[3], Y[3]; /* 16.16 snapped */
-    int64_t area_fx;    /* exact double area in 2^-32 px^2, >0 when coverable */
-    float inv_area_fx;
+    int64_t area_fx;    /* exact double area of the snapped triangle, 2^-32 px^2 */
+    float inv_area_ref; /* 1 / |cross(v0-v1, v0-v2)| of the float screen triangle */
     int visible;
     int float_path;
     int coverable_fx;
@@ -385,7 +385,7 @@ static void setup_fixed(tri_setup *t)
     t->float_path = !(in_guard(t->s[0]) && in_guard(t->s[1]) && in_guard(t->s[2]));
     t->coverable_fx = 0;
     t->area_fx = 0;
-    t->inv_area_fx = 0.f;
+    t->inv_area_ref = 0.f;
     if (t->float_path) return;
     for (int i = 0; i < 3; ++i) { t->X[i] = snap(t->s[i].x); t->Y[i] = snap(t->s[i].y); }
     /* S = E(v0; v1, v2) = cross(v0 - v1, v2 - v1); equals |cross(v0-v1, v0-v2)|
@@ -393,9 +393,14 @@ static void setup_fixed(tri_setup *t)
     const int64_t S = (int64_t)(t->X[0] - t->X[1]) * (int64_t)(t->Y[2] - t->Y[1]) -
                       (int64_t)(t->Y[0] - t->Y[1]) * (int64_t)(t->X[2] - t->X[1]);
     t->area_fx = S;
-    if (S > 0) {
+    /* the float area the reference divides by (CUDAROPs.cu:336); a triangle
+     * whose float area is 0 would give NaN weights and is not rasterised */
+    const v2 a = {t->s[0].x - t->s[1].x, t->s[0].y - t->s[1].y};
+    const v2 b = {t->s[0].x - t->s[2].x, t->s[0].y - t->s[2].y};
+    const float area = fabsf(fmaf(a.x, b.y, -(a.y * b.x)));
+    if (S > 0 && area > 0.f) {
         t->coverable_fx = 1;
-        t->inv_area_fx = 1.0f / (float)S;
+        t->inv_area_ref = 1.0f / area;
     }
 }
 
@@ -407,23 +412,10 @@ static int64_t edge_fx(int32_t px, int32_t py, int32_t ax, int32_t ay, int32_t b
     return dx * (int64_t)(by - ay) - dy * (int64_t)(bx - ax);
 }
 
-/* Fixed-point coverage; weights in the reference's order (CUDAROPs.cu:140-142):
- * w[2] from edge v0->v1, w[0] from v1->v2, w[1] from v2->v0. */
-static int cover_fixed(const tri_setup *t, int32_t px, int32_t py, float w[3])
-{
-    const int64_t e2 = edge_fx(px, py, t->X[0], t->Y[0], t->X[1], t->Y[1]);
-    const int64_t e0 = edge_fx(px, py, t->X[1], t->Y[1], t->X[2], t->Y[2]);
-    const int64_t e1 = edge_fx(px, py, t->X[2], t->Y[2], t->X[0], t->Y[0]);
-    if (e0 < 0 || e1 < 0 || e2 < 0) return 0;
-    w[0] = (float)e0 * t->inv_area_fx;
-    w[1] = (float)e1 * t->inv_area_fx;
-    w[2] = (float)e2 * t->inv_area_fx;
-    return 1;
-}
-
-/* Float coverage, IsPixelInTriangle + weight normalisation
- * (CUDAROPs.cu:120-145, 334-339). */
-static int cover_ref(const tri_setup *t, float px, float py, float w[3], float eraw[3])
+/* The reference's float edge functions at a pixel, weights order as
+ * IsPixelInTriangle (CUDAROPs.cu:120-142): w[2] from edge v0->v1, w[0] from
+ * v1->v2, w[1] from v2->v0. */
+static void edges_ref(const tri_setup *t, float px, float py, float w[3])
 {
     const v2 v0 = t->s[0], v1 = t->s[1], v2_ = t->s[2];
     const v2 ea = {v1.x - v0.x, v1.y - v0.y};
@@ -432,6 +424,31 @@ static int cover_ref(const tri_setup *t, float px, float py, float w[3], float e
     w[2] = fmaf(px - v0.x, ea.y, -((py - v0.y) * ea.x));
     w[0] = fmaf(px - v1.x, eb.y, -((py - v1.y) * eb.x));
     w[1] = fmaf(px - v2_.x, ec.y, -((py - v2_.y) * ec.x));
+}
+
+/* Fixed-point coverage (exact int64 edge functions of the 16.16 snapped
+ * triangle, inclusive); the interpolation weights are the reference's float
+ * edge values times 1/area, so depth and attributes follow the unsnapped
+ * triangle. */
+static int cover_fixed(const tri_setup *t, int32_t px, int32_t py, float w[3])
+{
+    const int64_t e2 = edge_fx(px, py, t->X[0], t->Y[0], t->X[1], t->Y[1]);
+    const int64_t e0 = edge_fx(px, py, t->X[1], t->Y[1], t->X[2], t->Y[2]);
+    const int64_t e1 = edge_fx(px, py, t->X[2], t->Y[2], t->X[0], t->Y[0]);
+    if (e0 < 0 || e1 < 0 || e2 < 0) return 0;
+    edges_ref(t, (float)px, (float)py, w);
+    w[0] = w[0] * t->inv_area_ref;
+    w[1] = w[1] * t->inv_area_ref;
+    w[2] = w[2] * t->inv_area_ref;
+    return 1;
+}
+
+/* Float coverage, IsPixelInTriangle + weight normalisation
+ * (CUDAROPs.cu:120-145, 334-339). */
+static int cover_ref(const tri_setup *t, float px, float py, float w[3], float eraw[3])
+{
+    const v2 v0 = t->s[0], v1 = t->s[1], v2_ = t->s[2];
+    edges_ref(t, px, py, w);
     if (eraw) { eraw[0] = w[0]; eraw[1] = w[1]; eraw[2] = w[2]; }
     if (!(w[0] >= 0.f && w[1] >= 0.f && w[2] >= 0.f)) return 0;
     const v2 a = {v0.x - v1.x, v0.y - v1.y}, b = {v0.x - v2_.x, v0.y - v2_.y};

@@ -158,7 +158,7 @@ def strip_scene():
     for j in range(ny - 1):
         row = []
         for i in range(nx):
-            row += [j * nx + i, (j + 1) * nx + i]
+            row += [(j + 1) * nx + i, j * nx + i]  # counter-clockwise in NDC: the covered winding
         if idx:
             idx += [idx[-1], row[0]]
         idx += row
@@ -183,7 +183,7 @@ def test_empty_scene_is_clear_colour(gbr_lib, cuda_device):
 
 def test_guard_band_triangles_use_float_edges(gbr_lib, cuda_device):
     v = np.zeros(6, scenes.POS3_RGBA8)
-    v["p"][0:3] = [(-0.5, -0.5, 0.4), (30.0, 0.2, 0.6), (-0.4, 0.7, 0.5)]  # x_ndc=30 -> far right of the band
+    v["p"][0:3] = [(-0.5, -0.5, 0.4), (80.0, 0.2, 0.6), (-0.4, 0.7, 0.5)]  # x_ndc=80 -> 12960 px, outside +-8192
     v["p"][3:6] = [(-0.9, -0.9, 0.2), (-0.9, 0.9, 0.9), (0.9, -0.9, 0.9)]
     v["rgba"] = [0xFF0000FF, 0xFF00FF00, 0xFFFF0000, 0xFF808080, 0xFF101010, 0xFFF0F0F0]
     s = scenes.Scene("guard", 320, 240, 16, 16, scenes.identity_camera(), [scenes.Mesh(vertices=v)],
