@@ -271,6 +271,26 @@ def run_ours(args, rank, world, local):
     return line
 
 
+def profile_frames(n: int):
+    """The benchmark's frame, device resident, n times on the default stream."""
+    import torch
+    import gbr
+
+    dev = torch.device("cuda", 0)
+    scene = make_scene(0)
+    mesh = scene.meshes[0]
+    d_vert = torch.from_numpy(mesh.vertices.view(np.uint8)).to(dev)
+    r = gbr.Renderer(WIDTH, HEIGHT)
+    r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, 256)
+    r.bind_mesh_device(d_vert.data_ptr(), len(mesh.vertices), mesh.vertex_format)
+    for _ in range(n):
+        r.render_scene(scene)
+    st = r.stats()
+    torch.cuda.synchronize(dev)
+    r.close()
+    print(json.dumps({"frames": n, "pairs": st["num_pairs"], "visible": st["num_visible"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -278,8 +298,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="render this many device-resident frames and exit (for a profiler)")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.profile_frames:
+        import build as gbr_build
+        gbr_build.build()
+        profile_frames(args.profile_frames)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

@@ -1,0 +1,95 @@
+"""The CUDA path against the reference's own output (tests/golden/*.npz,
+produced by the reference CUDARenderer on the GPU), and the C++ host API
+(include/gbr_cudarenderer.hpp) end to end.
+
+Bar: bin lists identical (sha256 of the sorted per-bin lists); visible
+triangle count identical; framebuffer within 1 LSB per channel and
+interpolated depth within 1e-6 relative, except at pixels where either
+(a) the winning triangle differs because a coverage decision flips inside
+the stated edge band (|e_ref| <= bound), or (b) the reference resolved a tie
+of integer depth keys by its atomic order.  Both are counted and printed.
+"""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import scenes
+from oracle import oracle
+from oracle.ref import ref_io
+from test_golden import FIXTURES, channels, load, scene_for
+import make_golden
+
+pytestmark = pytest.mark.gpu
+EMPTY = 0xFFFFFFFF
+
+
+def render_gpu(gbr, scene):
+    with gbr.Renderer(scene.width, scene.height) as r:
+        r.load_scene(scene)
+        r.render_scene(scene)
+        colour, depth = r.readback()
+        ids = r.readback_ids()
+        offsets, bins = r.get_bins()
+        st = r.stats()
+    return colour, depth, ids, offsets, bins, st
+
+
+@pytest.mark.skipif(not FIXTURES, reason="no golden fixtures")
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-4] for p in FIXTURES])
+def test_cuda_path_against_reference(gbr_lib, cuda_device, path):
+    meta, arrays = load(path)
+    scene = scene_for(meta)
+    colour, depth, ids, offsets, bins, st = render_gpu(gbr_lib, scene)
+    assert make_golden.bins_hash(offsets, bins) == meta["bins_sha256"], "bin lists differ from the reference"
+    assert st["num_visible"] == meta["visible"]
+    r0, r1 = meta["rows"]
+    dc = np.abs(channels(colour[r0:r1]) - channels(arrays["colour"])).max(-1)
+    zr = arrays["z"].astype(np.float64)
+    dz = np.abs(depth[r0:r1].astype(np.float64) - zr) > 1e-6 * np.maximum(np.abs(zr), 1e-30)
+    bad = np.argwhere((dc > 1) | dz)
+    oref = oracle.render(scene, oracle.RASTER_REFERENCE, want_bins=False) if len(bad) else None
+    band = ties = 0
+    for y, x in bad[:1000]:
+        py = int(r0 + y)
+        g, o = int(ids[py, x]), int(oref["ids"][py, x])
+        if g != o:
+            explained = False
+            for p in {g, o} - {EMPTY}:
+                pr = oracle.probe(scene, p, int(x), py)
+                if pr["covered_ref"] != pr["covered_fixed"] and any(
+                        abs(e) <= b for e, b in zip(pr["e_ref"], pr["e_bound"])):
+                    explained = True
+            if not explained and g != EMPTY and o != EMPTY:
+                zg, zo = float(depth[py, x]), float(oref["depth"][py, x])
+                explained = abs(zg - zo) <= 1e-6 * max(abs(zg), abs(zo))
+            assert explained, f"winner differs outside the edge band at {(int(x), py)}: ours {g}, reference-mode {o}"
+            band += 1
+        else:
+            key_g = int(np.float32(depth[py, x]) * np.float32(2 ** 31))
+            key_r = int(np.float32(arrays["z"][y, x]) * np.float32(2 ** 31))
+            assert key_g == key_r, f"same winner but z differs at {(int(x), py)}"
+            ties += 1
+    total = (r1 - r0) * meta["width"]
+    print(f"{meta['case']}: {len(bad)} of {total} pixels differ ({band} edge band, {ties} depth-key ties)")
+    assert len(bad) <= max(20, total // 500)
+
+
+def test_cpp_host_api_renders_like_the_c_abi(gbr_lib, cuda_device):
+    import build as gbr_build
+    exe = gbr_build.build_facade_demo()
+    scene = scenes.sphere_scene()
+    with tempfile.TemporaryDirectory() as td:
+        sp, op = os.path.join(td, "scene.bin"), os.path.join(td, "out.bin")
+        ref_io.write_scene(scene, sp)
+        p = subprocess.run([exe, sp, op], capture_output=True, text=True)
+        assert p.returncode == 0, p.stderr
+        raw = np.fromfile(op, np.uint32)
+    w, h = int(raw[0]), int(raw[1])
+    colour = raw[2:2 + w * h].reshape(h, w)
+    depth = raw[2 + w * h:].view(np.float32).reshape(h, w)
+    c2, d2, _, _, _, _ = render_gpu(gbr_lib, scene)
+    assert np.array_equal(colour, c2) and np.array_equal(depth.view(np.uint32), d2.view(np.uint32))
+    assert "1256 of 3968 triangles visible" in p.stdout
