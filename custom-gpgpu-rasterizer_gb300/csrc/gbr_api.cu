@@ -79,6 +79,10 @@ void mat4_mul(const float* lm, const float* rm, float* out) {
 
 }  // namespace
 
+// Lets other translation units of the library report through
+// gbr_last_error_string().
+void gbr::set_last_error(const char* msg) { g_last_error = msg; }
+
 struct gbr_renderer {
     int device = 0;
     int num_sms = 0;

@@ -14,4 +14,7 @@ cudaError_t launch_fill(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s);
 cudaError_t launch_clear(const FrameDev& F, cudaStream_t s);
 
+// Message returned by gbr_last_error_string() on the calling thread.
+void set_last_error(const char* msg);
+
 }  // namespace gbr

@@ -32,7 +32,7 @@ EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "g
             "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
             "gbr_texture_upload", "gbr_texture_remove", "gbr_set_binning", "gbr_set_bin_capacity",
             "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
-            "gbr_get_bins", "gbr_get_stats", "gbr_last_error_string", "gbr_version"]
+            "gbr_get_bins", "gbr_get_stats", "gbr_render_noalloc", "gbr_last_error_string", "gbr_version"]
 
 
 class GbrError(RuntimeError):
@@ -89,6 +89,8 @@ def lib():
             "gbr_device_buffers": [vp, C.POINTER(vp), C.POINTER(vp)],
             "gbr_get_bins": [vp, vp, vp, u64, C.POINTER(u64), vp],
             "gbr_get_stats": [vp, C.POINTER(Stats), vp],
+            "gbr_render_noalloc": [vp, u32, u32, vp, u32, u32, vp, C.POINTER(Camera), u32, u32, u32, u32, u32, u32,
+                                   u32, u32, u32, u32, vp, vp, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

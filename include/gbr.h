@@ -151,6 +151,28 @@ gbr_status gbr_get_bins(gbr_renderer *r, uint32_t *offsets, uint32_t *ids, uint6
  * (CUDARenderer.h:63-73); synchronises with `stream`. */
 gbr_status gbr_get_stats(gbr_renderer *r, gbr_stats *out, void *stream);
 
+/* No counterpart in the reference.  Renders one frame of one mesh (vertex
+ * colours; no textures) from device-resident vertices into caller-owned
+ * device buffers (width*height colour words and depths) without allocating
+ * any device memory, for callers that may not allocate while they render:
+ * hosts with a fixed device-memory budget that forbid library allocations,
+ * real-time loops that cannot take cudaMalloc's implicit synchronisation,
+ * processes under a hard memory cap.  Its scratch is one static device
+ * array of about 20 MiB that every GPU loading the library holds until
+ * exit.  Limits: <= 65536 triangles, <= 2^20 pixels, <= 4096 bins of
+ * <= 64x64 px, queue_chunk >= 64, <= 2^20 (triangle, bin) entries; larger
+ * inputs return GBR_ERR_INVALID_ARG (or GBR_ERR_OUT_OF_MEMORY for the
+ * entry count, found after the frame).  The first call on a device sets up
+ * its scratch address and should come before any stream capture.  Calls
+ * share the scratch: calls whose GPU work overlaps race.  Returns after
+ * synchronising `stream`. */
+gbr_status gbr_render_noalloc(const void *d_vertices, uint32_t num_vertices, uint32_t vertex_format,
+                              const uint32_t *d_indices, uint32_t num_indices, uint32_t topology,
+                              const float world[16], const gbr_camera *cam, uint32_t width, uint32_t height,
+                              uint32_t num_bins_x, uint32_t num_bins_y, uint32_t bin_w, uint32_t bin_h,
+                              uint32_t queue_chunk, uint32_t cull, uint32_t sample, uint32_t vis,
+                              uint32_t *d_colour, float *d_depth, void *stream);
+
 const char *gbr_last_error_string(void);
 /* Library version, e.g. 0x000100 for 0.1.0. */
 uint32_t gbr_version(void);
