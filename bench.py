@@ -41,6 +41,7 @@ import numpy as np  # noqa: E402
 
 N_TRI = 1_000_000
 WIDTH, HEIGHT, BIN = 1920, 1080, 16
+CHUNK = 4096
 METRIC = "triangles/s (1M-tri 1080p soup frame, exact two-pass binning)"
 UNIT = "triangles/s"
 WORKLOAD = "soup-1M-1080p"
@@ -171,7 +172,7 @@ def run_ours(args, rank, world, local):
 
     # device-resident frame ---------------------------------------------------
     r = gbr.Renderer(WIDTH, HEIGHT)
-    r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, 256)
+    r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, CHUNK)
     r.bind_mesh_device(d_vert.data_ptr(), nv, mesh.vertex_format)
     r.set_timing(True)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
@@ -210,7 +211,7 @@ def run_ours(args, rank, world, local):
 
     # end to end through the C ABI with host buffers -----------------------
     r2 = gbr.Renderer(WIDTH, HEIGHT)
-    r2.load_scene(scene)
+    r2.load_scene(scene, CHUNK)
     host_v = torch.from_numpy(mesh.vertices.view(np.uint8).copy()).pin_memory()
     host_c = torch.empty(WIDTH * HEIGHT, dtype=torch.int32).pin_memory()
     colour_np = host_c.numpy().view(np.uint32)
@@ -250,7 +251,7 @@ def run_ours(args, rank, world, local):
                 "warmup": args.warmup, "ms_per_step": t_frame * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded soup per rank)",
                 "config": {"workload": WORKLOAD, "triangles": N_TRI, "resolution": [WIDTH, HEIGHT],
-                           "bins": [BIN, BIN], "queue_chunk": 256, "binning": "exact two-pass",
+                           "bins": [BIN, BIN], "queue_chunk": CHUNK, "binning": "exact two-pass",
                            "l2": "256 MB write between timed frames", "pairs": int(pairs),
                            "frames_per_s": world / t_frame,
                            "ms_setup": statistics.mean(ms_setup), "ms_bin": statistics.mean(ms_bin),
@@ -281,7 +282,7 @@ def profile_frames(n: int):
     mesh = scene.meshes[0]
     d_vert = torch.from_numpy(mesh.vertices.view(np.uint8)).to(dev)
     r = gbr.Renderer(WIDTH, HEIGHT)
-    r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, 256)
+    r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, CHUNK)
     r.bind_mesh_device(d_vert.data_ptr(), len(mesh.vertices), mesh.vertex_format)
     for _ in range(n):
         r.render_scene(scene)

@@ -397,7 +397,7 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
         return fail(GBR_ERR_INVALID_ARG, "bins %ux%u of %ux%u px: need >= 1 bin of 1..%d px", num_bins_x, num_bins_y,
                     bin_w, bin_h, kMaxBinDim);
     if (num_bins_x > 32767u || num_bins_y > 32767u) return fail(GBR_ERR_INVALID_ARG, "too many bins");
-    if (queue_chunk == 0) queue_chunk = 256;
+    if (queue_chunk == 0) queue_chunk = 4096;
     cudaDeviceSynchronize();
     free_bins(r);
     r->nbx = num_bins_x; r->nby = num_bins_y; r->bw = bin_w; r->bh = bin_h; r->chunk = queue_chunk;

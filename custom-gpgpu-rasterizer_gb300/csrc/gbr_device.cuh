@@ -23,6 +23,7 @@ constexpr uint32_t kFlagFloat = 2u;               // outside the guard band: flo
 constexpr int kMaxBinDim = 64;
 constexpr int kRasterThreads = 256;
 constexpr int kBatch = 256;
+constexpr uint32_t kPhase = 64;                   // triangles between hierarchical-z refreshes
 
 enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
 

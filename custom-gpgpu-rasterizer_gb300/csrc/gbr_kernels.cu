@@ -230,15 +230,41 @@ struct RasterShared {
     TriSetup rec[kBatch];
     uint32_t prim[kBatch];
     uint32_t warp_count[kRasterThreads / 32];
+    uint32_t warp_max[kRasterThreads / 32];
     uint32_t item[4];
     int next;
     int nv;
     int last;
-    int pad;
+    uint32_t tile_max;   // max depth key over the tile's pixels (0xFFFFFFFF while any pixel is empty)
 };
 
+// Lower bound of the depth keys any fragment of the triangle can produce.
+// A pixel covered under the 16.16 rule is at most the snapping distance
+// outside the float triangle, so each float edge value there is at least
+// -beta with beta <= 3*2^-17*D + 2^-32 + 2^-20*D^2 (D = the triangle's
+// x + y extent; snapping moves vertices <= 2^-17 px; the float evaluation
+// errs by <= 4 ulp of its product terms), and the three edge values sum to
+// the float area within 2^-20*D^2 each.  With g = (2^-15*D + 2^-32 +
+// 2^-18*D^2)/area, every weight is >= -g and the weights sum to 1 +- g, so
+// z >= zmin*(1-g) - (3g + 2^-22)*max|z_i| when zmin >= 0 (2^-22 covers the
+// rounding of the fused z chain).  The key of that bound never exceeds the
+// key of a fragment of the triangle.
+__device__ __forceinline__ bool hiz_reject(const TriSetup& t, int minx, int maxx, int miny, int maxy,
+                                           uint32_t tile_max) {
+    if (tile_max == 0xFFFFFFFFu) return false;
+    const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
+    if (!(zmin >= 0.f)) return false;
+    const float zabs = fmaxf(fabsf(t.z0), fmaxf(fabsf(t.z1), fabsf(t.z2)));
+    const float D = (float)((maxx - minx) + (maxy - miny)) * (1.0f / 65536.f) + 1.f;
+    const float g = (D * 3.0517578125e-05f + 2.3283064365386963e-10f + D * D * 3.814697265625e-06f) * t.inv_area;
+    const float zb = zmin * (1.f - g) - (3.f * g + 2.384185791015625e-07f) * zabs;
+    if (!(zb > 0.f)) return false;
+    if (zb >= 1.f) return true;
+    return (uint32_t)__float2int_rz(__fmul_rn(zb, 2147483648.0f)) > tile_max;
+}
+
 __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
-                                             int ty0, int tw, int th, uint32_t lane) {
+                                             int ty0, int tw, int th, uint32_t lane, uint32_t tile_max) {
     const int X0 = snap_fx(t.x0), Y0 = snap_fx(t.y0), X1 = snap_fx(t.x1);
     const int Y1 = snap_fx(t.y1), X2 = snap_fx(t.x2), Y2 = snap_fx(t.y2);
     const int minx = min(X0, min(X1, X2)), maxx = max(X0, max(X1, X2));
@@ -247,6 +273,7 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
     const int px0 = max((minx + 0xFFFF) >> kFxBits, tx0), px1 = min(maxx >> kFxBits, tx0 + tw - 1);
     const int py0 = max((miny + 0xFFFF) >> kFxBits, ty0), py1 = min(maxy >> kFxBits, ty0 + th - 1);
     if (px0 > px1 || py0 > py1) return;
+    if (hiz_reject(t, minx, maxx, miny, maxy, tile_max)) return;
     const int bwid = px1 - px0 + 1;
     const int lsw = bwid <= 1 ? 0 : bwid <= 2 ? 1 : bwid <= 4 ? 2 : bwid <= 8 ? 3 : bwid <= 16 ? 4 : 5;
     const int sw = 1 << lsw, sh = 32 >> lsw;
@@ -379,14 +406,35 @@ __global__ void __launch_bounds__(kRasterThreads, 2) raster_kernel(FrameDev F) {
                 S.prim[pos] = e;
             }
             __syncthreads();
-            for (;;) {
-                int i = 0;
-                if (lane == 0) i = atomicAdd(&S.next, 1);
-                i = __shfl_sync(0xFFFFFFFFu, i, 0);
-                if (i >= (int)total) break;
-                const TriSetup& t = S.rec[i];
-                if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
-                else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
+            // phases of kPhase triangles; the tile's max depth key is refreshed
+            // between phases for the hierarchical-z test
+            for (uint32_t p0 = 0; p0 < total; p0 += kPhase) {
+                const uint32_t p1 = min(total, p0 + kPhase);
+                if (b0 > 0 || p0 > 0) {
+                    uint32_t m = 0;
+                    for (int i = (int)tid; i < npx; i += kRasterThreads)
+                        m = max(m, (uint32_t)(tile[i] >> 32));
+                    m = __reduce_max_sync(0xFFFFFFFFu, m);
+                    if (lane == 0) S.warp_max[warp] = m;
+                }
+                if (tid == 0) S.next = (int)p0;
+                __syncthreads();
+                uint32_t tile_max = 0xFFFFFFFFu;
+                if (b0 > 0 || p0 > 0) {
+                    tile_max = 0;
+#pragma unroll
+                    for (uint32_t w = 0; w < kRasterThreads / 32; ++w) tile_max = max(tile_max, S.warp_max[w]);
+                }
+                for (;;) {
+                    int i = 0;
+                    if (lane == 0) i = atomicAdd(&S.next, 1);
+                    i = __shfl_sync(0xFFFFFFFFu, i, 0);
+                    if (i >= (int)p1) break;
+                    const TriSetup& t = S.rec[i];
+                    if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
+                    else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane, tile_max);
+                }
+                __syncthreads();
             }
         }
         __syncthreads();

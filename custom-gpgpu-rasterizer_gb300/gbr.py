@@ -156,7 +156,7 @@ class Renderer:
         self.close()
 
     # -- setup ---------------------------------------------------------
-    def setup_bins(self, nbx: int, nby: int, bw: int, bh: int, chunk: int = 256):
+    def setup_bins(self, nbx: int, nby: int, bw: int, bh: int, chunk: int = 4096):
         check(self._lib.gbr_setup_bins(self.h, nbx, nby, bw, bh, chunk))
         self.nbx, self.nby = nbx, nby
 
@@ -197,7 +197,7 @@ class Renderer:
     def clear_scene(self):
         check(self._lib.gbr_scene_clear(self.h))
 
-    def load_scene(self, scene, chunk: int = 256):
+    def load_scene(self, scene, chunk: int = 4096):
         """LoadScene: bins from the scene, textures, meshes."""
         self.setup_bins(scene.num_bins_x, scene.num_bins_y, scene.bin_w, scene.bin_h, chunk)
         self.clear_scene()
