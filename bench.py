@@ -262,10 +262,131 @@ def run_ours(args, rank, world, local):
                              "peak_source": peak_kind, "algorithmic_bytes_per_launch": raster_bytes},
                 "e2e": {"value": world * N_TRI / t_e2e, "unit": UNIT, "h2d_bytes_per_step": vbytes,
                         "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
-                "gpu_launches": 4 * args.steps,
+                "gpu_launches": 5 * args.steps,
                 "clocks": clocks,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return line
+
+
+BATCH_SCENES = 256
+BATCH_METRIC = "triangles/s (256 uneven soups, one batched frame)"
+
+
+def run_batch(args, rank, world, local):
+    """The batched workload: 256 seeded soups (1k-500k triangles, resolutions
+    256^2 .. 1920x1080), one graph-replayed launch chain per batch frame, bin
+    size / queue chunk / raster variant chosen by the autotuner; beside it,
+    the same scenes rendered one frame per scene on the same stream."""
+    import torch
+    import gbr
+    import scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sl = scenes.batch_scenes(BATCH_SCENES, seed=rank)
+    n_tri = sum(s.num_triangles for s in sl)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    rs = []
+    for s in sl:
+        r = gbr.Renderer(s.width, s.height)
+        r.load_scene(s, CHUNK)
+        rs.append(r)
+    b = gbr.Batch()
+    for r, s in zip(rs, sl):
+        b.add_scene(r, s)
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        best = b.autotune(bin_sizes=(8, 16, 32), chunks=(32, 64, 128), raster_ctas=(4, 5, 6), frames=2, stream=sptr)
+    t_tune = time.perf_counter() - t0
+    b.set_timing(True)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            b.render(sptr)
+        st = b.stats(sptr)
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(local)
+    ms = []
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            b.render(sptr)
+            st = b.stats(sptr)
+            ms.append(st["ms_frame"])
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    t_batch = statistics.mean(ms) / 1e3
+
+    # the same scenes, one single-scene frame each, back to back on the stream
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for r, s in zip(rs, sl):
+            r.render_scene(s, sptr)
+        seq = []
+        for _ in range(max(2, args.steps // 4)):
+            flush.zero_()
+            ev0.record(stream)
+            for r, s in zip(rs, sl):
+                r.render_scene(s, sptr)
+            ev1.record(stream)
+            ev1.synchronize()
+            seq.append(ev0.elapsed_time(ev1))
+    t_seq = statistics.mean(seq) / 1e3
+
+    # end to end: vertices from pinned host memory, batch frame, colour back
+    hosts = [torch.from_numpy(s.meshes[0].vertices.view(np.uint8).copy()).pin_memory() for s in sl]
+    outs = [torch.empty(s.width * s.height, dtype=torch.int32).pin_memory() for s in sl]
+    h2d = sum(h.numel() for h in hosts)
+    d2h = sum(o.numel() * 4 for o in outs)
+    e2e = []
+    with torch.cuda.stream(stream):
+        for step in range(args.warmup + args.steps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for r, h, s in zip(rs, hosts, sl):
+                r.update_vertices(0, h.data_ptr(), len(s.meshes[0].vertices), sptr)
+            b.render(sptr)
+            for i, o in enumerate(outs):
+                gbr.check(b._lib.gbr_batch_readback(b.h, i, gbr.C.c_void_p(o.data_ptr()), None, None,
+                                                    gbr.C.c_void_p(sptr)))
+            if step >= args.warmup:
+                e2e.append(time.perf_counter() - t0)
+    t_e2e = statistics.mean(e2e)
+    if dist:
+        tt = torch.tensor([t_batch, t_e2e, t_seq], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_batch, t_e2e, t_seq = (float(x) for x in tt.tolist())
+    line = None
+    if rank == 0:
+        line = {"metric": BATCH_METRIC, "value": world * n_tri / t_batch, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded soups per rank)",
+                "config": {"workload": "batch-256-uneven-soups", "scenes": BATCH_SCENES, "triangles": n_tri,
+                           "pixels": int(sum(s.width * s.height for s in sl)), "tuned": best,
+                           "autotune_s": t_tune, "pairs": int(st["num_pairs"]),
+                           "work_items": int(st["num_work_items"]), "graph_captures": int(st["graph_captures"]),
+                           "batch_frames_per_s": 1.0 / t_batch,
+                           "per_scene_frames_ms": t_seq * 1e3,
+                           "per_scene_triangles_per_s": world * n_tri / t_seq,
+                           "batch_speedup_vs_per_scene": t_seq / t_batch,
+                           "l2": "256 MB write between timed frames"},
+                "e2e": {"value": world * n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": 6 * args.steps,
+                "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    b.close()
+    for r in rs:
+        r.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -299,6 +420,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["soup", "batch"], default="soup",
+                    help="soup: the 1M-triangle 1080p frame; batch: 256 uneven soups as one batched frame")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="render this many device-resident frames and exit (for a profiler)")
     args = ap.parse_args()
@@ -317,7 +440,10 @@ def main():
     else:
         while not gbr_build.up_to_date():
             time.sleep(1)
-    run_ours(args, rank, world, local)
+    if args.workload == "batch":
+        run_batch(args, rank, world, local)
+    else:
+        run_ours(args, rank, world, local)
 
 
 if __name__ == "__main__":

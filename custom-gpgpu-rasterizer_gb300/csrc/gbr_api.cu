@@ -16,15 +16,17 @@
 #include <vector>
 
 #include "../../include/gbr.h"
+#include "gbr_internal.h"
 #include "gbr_kernels.h"
+#include "gbr_predict.h"
 
 using namespace gbr;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
 
-gbr_status fail(gbr_status st, const char* fmt, ...) {
+gbr_status gbr::fail(gbr_status st, const char* fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -34,37 +36,11 @@ gbr_status fail(gbr_status st, const char* fmt, ...) {
     return st;
 }
 
-#define GBR_CUDA(call)                                                                                  \
-    do {                                                                                                \
-        cudaError_t e_ = (call);                                                                        \
-        if (e_ != cudaSuccess) return fail(GBR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
-    } while (0)
+// Lets other translation units of the library report through
+// gbr_last_error_string().
+void gbr::set_last_error(const char* msg) { g_last_error = msg; }
 
-struct MeshHost {
-    bool owned = false;
-    void* d_vertices = nullptr;
-    uint32_t* d_indices = nullptr;
-    uint32_t num_vertices = 0, num_indices = 0, vertex_format = 0, topology = 0;
-    uint64_t num_tris = 0;
-    float world[16];
-    int32_t tex_ids[4] = {-1, -1, -1, -1};
-};
-
-struct TexHost {
-    uint32_t* d_px = nullptr;
-    uint32_t w = 0, h = 0;
-};
-
-uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_indices, uint32_t topology) {
-    if (!indices) return num_vertices / 3u;
-    if (topology == GBR_TOPOLOGY_TRIANGLE_LIST) return num_indices / 3u;
-    return num_indices >= 2u ? num_indices - 2u : 0u;
-}
-
-// Matrix<4,4>::operator*(Matrix<4,4>) (Matrix4.h:120-143) on the host, left
-// to right with no fused multiply-add (built with -ffp-contract=off), as the
-// reference computes WVP.
-void mat4_mul(const float* lm, const float* rm, float* out) {
+void gbr::mat4_mul(const float* lm, const float* rm, float* out) {
     float t[16];
     for (int r = 0; r < 4; ++r)
         for (int c = 0; c < 4; ++c) {
@@ -77,66 +53,84 @@ void mat4_mul(const float* lm, const float* rm, float* out) {
     memcpy(out, t, sizeof t);
 }
 
+namespace {
+
+TexDev tex_dev(const gbr_renderer* r, int32_t id) {
+    TexDev t{nullptr, 0u, 0u};
+    if (id >= 0 && (size_t)id < r->textures.size() && r->textures[id].d_px) {
+        t.px = r->textures[id].d_px;
+        t.w = r->textures[id].w;
+        t.h = r->textures[id].h;
+    }
+    return t;
+}
+
 }  // namespace
 
-// Lets other translation units of the library report through
-// gbr_last_error_string().
-void gbr::set_last_error(const char* msg) { g_last_error = msg; }
+uint64_t gbr::scene_triangles(const gbr_renderer* r) {
+    uint64_t n = 0;
+    for (const MeshHost& m : r->meshes) n += m.num_tris;
+    return n;
+}
 
-struct gbr_renderer {
-    int device = 0;
-    int num_sms = 0;
-    uint32_t W = 0, H = 0;
-    uint32_t nbx = 0, nby = 0, bw = 0, bh = 0, chunk = 256;
-    bool bins_ready = false;
-    uint32_t binning = GBR_BINNING_EXACT;
-    bool timing = false;
-    int raster_blocks_per_sm = 1;
+void gbr::build_mesh_table(const gbr_renderer* r, const gbr_camera* cam, MeshDev* out) {
+    float vp[16];
+    mat4_mul(cam->proj, cam->view, vp);
+    uint32_t base = 0;
+    for (size_t i = 0; i < r->meshes.size(); ++i) {
+        const MeshHost& m = r->meshes[i];
+        MeshDev& d = out[i];
+        memset(&d, 0, sizeof d);
+        d.vertices = m.d_vertices;
+        d.indices = m.d_indices;
+        d.vertex_format = m.vertex_format;
+        d.topology = m.topology;
+        d.num_vertices = m.num_vertices;
+        d.num_tris = (uint32_t)m.num_tris;
+        d.prim_base = base;
+        base += (uint32_t)m.num_tris;
+        mat4_mul(vp, m.world, d.wvp);
+        memcpy(d.world, m.world, sizeof d.world);
+        // UpdateCUDAMeshTextures (CUDARenderer.cu:549-573): normal needs
+        // diffuse; specular and gloss need normal
+        const TexDev diff = tex_dev(r, m.tex_ids[0]);
+        if (diff.px) {
+            d.tex[0] = diff;
+            const TexDev norm = tex_dev(r, m.tex_ids[1]);
+            if (norm.px) {
+                d.tex[1] = norm;
+                d.tex[2] = tex_dev(r, m.tex_ids[2]);
+                d.tex[3] = tex_dev(r, m.tex_ids[3]);
+            }
+        }
+    }
+}
 
-    std::vector<MeshHost> meshes;
-    std::vector<TexHost> textures;
-
-    uint32_t* d_colour = nullptr;
-    float* d_depth = nullptr;
-    uint32_t* d_ids = nullptr;
-    unsigned long long* d_gvis = nullptr;
-
-    uint32_t* d_counts = nullptr;
-    uint32_t* d_offsets = nullptr;
-    uint32_t* d_cursors = nullptr;
-    uint32_t* d_capacity = nullptr;
-    uint32_t* d_bin_done = nullptr;
-    uint4* d_items = nullptr;
-    uint32_t items_cap = 0;
-    uint32_t* d_list = nullptr;
-    uint64_t list_cap = 0;
-
-    TriSetup* d_setup = nullptr;
-    uint2* d_rects = nullptr;
-    uint64_t tri_cap = 0;
-
-    MeshDev* d_meshes = nullptr;
-    MeshDev* h_meshes = nullptr;
-    uint32_t meshes_cap = 0;
-    std::vector<MeshDev> last_uploaded;
-    cudaEvent_t meshes_evt = nullptr;
-
-    Ctl* d_ctl = nullptr;
-    Ctl* h_ctl = nullptr;
-
-    bool have_frame = false;
-    gbr_camera last_cam{};
-    uint32_t last_cull = 0, last_sample = 0, last_vis = 0;
-    uint32_t overflow_reruns = 0;
-    cudaEvent_t ev[5] = {};
-    bool ev_recorded = false;
-};
+void gbr::frame_basics(const gbr_renderer* r, const gbr_camera* cam, uint32_t cull, uint32_t sample, uint32_t vis,
+                       FrameDev& F) {
+    memset(&F, 0, sizeof F);
+    F.width = r->W; F.height = r->H;
+    F.cull = cull; F.sample = sample; F.vis = vis; F.clear_colour32 = 0x003F3F3Fu;
+    F.num_meshes = (uint32_t)r->meshes.size();
+    F.num_tris = (uint32_t)scene_triangles(r);
+    for (int k = 0; k < 3; ++k) { F.cam_pos[k] = cam->pos[k]; F.cam_fwd[k] = cam->fwd[k]; }
+    F.colour = r->d_colour; F.depth = r->d_depth; F.ids = r->d_ids; F.gvis = r->d_gvis;
+}
 
 namespace {
+
+uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_indices, uint32_t topology) {
+    if (!indices) return num_vertices / 3u;
+    if (topology == GBR_TOPOLOGY_TRIANGLE_LIST) return num_indices / 3u;
+    return num_indices >= 2u ? num_indices - 2u : 0u;
+}
 
 void free_bins(gbr_renderer* r) {
     cudaFree(r->d_counts); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
     cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list);
+    cudaFree(r->d_feat); cudaFree(r->d_features_out);
+    r->d_feat = nullptr;
+    r->d_features_out = nullptr;
     r->d_counts = r->d_offsets = r->d_cursors = r->d_capacity = r->d_bin_done = r->d_list = nullptr;
     r->d_items = nullptr;
     r->items_cap = 0;
@@ -198,16 +192,6 @@ gbr_status ensure_meshes(gbr_renderer* r, uint32_t n) {
     return GBR_OK;
 }
 
-TexDev tex_dev(const gbr_renderer* r, int32_t id) {
-    TexDev t{nullptr, 0u, 0u};
-    if (id >= 0 && (size_t)id < r->textures.size() && r->textures[id].d_px) {
-        t.px = r->textures[id].d_px;
-        t.w = r->textures[id].w;
-        t.h = r->textures[id].h;
-    }
-    return t;
-}
-
 gbr_status validate_mesh_args(const void* vertices, uint32_t num_vertices, uint32_t vertex_format,
                               const uint32_t* indices, uint32_t num_indices, uint32_t topology, const float* world) {
     if (!vertices && num_vertices) return fail(GBR_ERR_INVALID_ARG, "vertices is null");
@@ -235,37 +219,8 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     if (st != GBR_OK) return st;
 
     // per-mesh descriptors with the matrices of this frame
-    float vp[16];
-    mat4_mul(cam->proj, cam->view, vp);
     std::vector<MeshDev> md(r->meshes.size());
-    uint32_t base = 0;
-    for (size_t i = 0; i < r->meshes.size(); ++i) {
-        const MeshHost& m = r->meshes[i];
-        MeshDev& d = md[i];
-        memset(&d, 0, sizeof d);
-        d.vertices = m.d_vertices;
-        d.indices = m.d_indices;
-        d.vertex_format = m.vertex_format;
-        d.topology = m.topology;
-        d.num_vertices = m.num_vertices;
-        d.num_tris = (uint32_t)m.num_tris;
-        d.prim_base = base;
-        base += (uint32_t)m.num_tris;
-        mat4_mul(vp, m.world, d.wvp);
-        memcpy(d.world, m.world, sizeof d.world);
-        // UpdateCUDAMeshTextures (CUDARenderer.cu:549-573): normal needs
-        // diffuse; specular and gloss need normal
-        const TexDev diff = tex_dev(r, m.tex_ids[0]);
-        if (diff.px) {
-            d.tex[0] = diff;
-            const TexDev norm = tex_dev(r, m.tex_ids[1]);
-            if (norm.px) {
-                d.tex[1] = norm;
-                d.tex[2] = tex_dev(r, m.tex_ids[2]);
-                d.tex[3] = tex_dev(r, m.tex_ids[3]);
-            }
-        }
-    }
+    if (!md.empty()) build_mesh_table(r, cam, md.data());
     const bool same = md.size() == r->last_uploaded.size() &&
                       (md.empty() || memcmp(md.data(), r->last_uploaded.data(), md.size() * sizeof(MeshDev)) == 0);
     if (!same && !md.empty()) {
@@ -277,30 +232,52 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     }
 
     FrameDev F;
-    memset(&F, 0, sizeof F);
-    F.width = r->W; F.height = r->H;
+    frame_basics(r, cam, cull, sample, vis, F);
     F.nbx = r->nbx; F.nby = r->nby; F.bw = r->bw; F.bh = r->bh; F.num_bins = nb;
-    F.cull = cull; F.sample = sample; F.vis = vis; F.clear_colour32 = 0x003F3F3Fu;
-    F.num_meshes = (uint32_t)r->meshes.size();
-    F.num_tris = (uint32_t)ntris;
     F.chunk = r->chunk;
-    for (int k = 0; k < 3; ++k) { F.cam_pos[k] = cam->pos[k]; F.cam_fwd[k] = cam->fwd[k]; }
+    F.phase = r->raster_phase;
+    F.raster_ctas = r->raster_ctas;
     F.meshes = r->d_meshes;
     F.setup = r->d_setup; F.rects = r->d_rects;
     F.counts = r->d_counts; F.offsets = r->d_offsets; F.cursors = r->d_cursors; F.capacity = r->d_capacity;
     F.bin_done = r->d_bin_done;
     F.items = r->d_items; F.items_cap = r->items_cap;
     F.list = r->d_list; F.list_cap = r->list_cap;
-    F.colour = r->d_colour; F.depth = r->d_depth; F.ids = r->d_ids; F.gvis = r->d_gvis;
     F.ctl = r->d_ctl;
+    const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
+    F.feat = r->d_feat;
+    F.mlp_w = r->d_mlp_w;
+    F.features_out = r->collect ? r->d_features_out : nullptr;
+    F.cap_alpha = r->cap_alpha; F.cap_beta = r->cap_beta; F.cap_gamma = r->cap_gamma;
+    F.sample_stride = kSampleStride;
+    F.exact_guard = predicted ? 1u : 0u;
 
     if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[0], s));
     GBR_CUDA(cudaMemsetAsync(r->d_ctl, 0, sizeof(Ctl), s));
-    if ((uint64_t)r->nbx * r->bw < r->W || (uint64_t)r->nby * r->bh < r->H) GBR_CUDA(launch_clear(F, s));
-    GBR_CUDA(launch_setup(F, false, s));
-    if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
-    GBR_CUDA(launch_scan(F, false, s));
-    GBR_CUDA(launch_fill(F, s));
+    if (predicted) {
+        // coarse pre-pass -> capacities -> one fused setup + fill pass; the
+        // exact kernels behind it only run if a bin overflowed
+        GBR_CUDA(launch_prepass(F, s));
+        GBR_CUDA(launch_capacity(F, true, s));
+        GBR_CUDA(launch_scan(F, true, s));
+        GBR_CUDA(launch_setup(F, true, s));
+        if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
+        GBR_CUDA(launch_items(F, s));
+        GBR_CUDA(launch_setup(F, false, s));
+        GBR_CUDA(launch_scan(F, false, s));
+        GBR_CUDA(launch_fill(F, s));
+    } else {
+        if (r->collect) {
+            GBR_CUDA(launch_prepass(F, s));
+            GBR_CUDA(launch_capacity(F, false, s));
+            GBR_CUDA(launch_feat_reset(F, s));
+        }
+        GBR_CUDA(launch_setup(F, false, s));
+        if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
+        GBR_CUDA(launch_scan(F, false, s));
+        GBR_CUDA(launch_fill(F, s));
+    }
+    r->last_predicted = predicted;
     if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[2], s));
     GBR_CUDA(launch_raster(F, (uint32_t)(r->num_sms * r->raster_blocks_per_sm), s));
     if (r->timing) {
@@ -329,6 +306,11 @@ gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
         GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     }
     if (r->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "bin storage overflow persists");
+    // predicted capacities that did not fit the list: grow it for the next frames
+    if (r->last_predicted && r->h_ctl->pred_capacity > r->list_cap) {
+        gbr_status st = ensure_list(r, r->h_ctl->pred_capacity);
+        if (st != GBR_OK) return st;
+    }
     return GBR_OK;
 }
 
@@ -375,12 +357,13 @@ gbr_status gbr_create(uint32_t width, uint32_t height, gbr_renderer** out) {
 
 gbr_status gbr_destroy(gbr_renderer* r) {
     if (!r) return GBR_OK;
+    if (r->in_batches) return fail(GBR_ERR_INVALID_ARG, "the renderer is in %u batch(es): destroy them first", r->in_batches);
     cudaDeviceSynchronize();
     gbr_scene_clear(r);
     for (TexHost& t : r->textures) cudaFree(t.d_px);
     free_bins(r);
     cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis);
-    cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_meshes); cudaFree(r->d_ctl);
+    cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_meshes); cudaFree(r->d_ctl); cudaFree(r->d_mlp_w);
     cudaFreeHost(r->h_meshes); cudaFreeHost(r->h_ctl);
     if (r->meshes_evt) cudaEventDestroy(r->meshes_evt);
     for (int i = 0; i < 5; ++i)
@@ -411,8 +394,13 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     GBR_CUDA(cudaMemset(r->d_capacity, 0, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_bin_done, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_bin_done, 0, nb * sizeof(uint32_t)));
+    // pre-pass accumulators: slot 4 (depth min) starts at all ones, the rest at 0
+    GBR_CUDA(cudaMalloc(&r->d_feat, (size_t)kFeatSlots * nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_feat, 0, (size_t)kFeatSlots * nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_feat + 4u * nb, 0xFF, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_features_out, (size_t)kFeatures * nb * sizeof(float)));
     int bps = 0;
-    GBR_CUDA(raster_configure(bin_w, bin_h, &bps));
+    GBR_CUDA(raster_configure(bin_w, bin_h, r->raster_ctas, &bps));
     r->raster_blocks_per_sm = std::max(bps, 1);
     r->bins_ready = true;
     r->have_frame = false;
@@ -556,11 +544,16 @@ gbr_status gbr_set_binning(gbr_renderer* r, uint32_t method) {
     return GBR_OK;
 }
 
-gbr_status gbr_set_bin_capacity(gbr_renderer* r, const uint32_t* capacity, int is_device, void* stream) {
-    if (!r || !capacity || !r->bins_ready) return fail(GBR_ERR_INVALID_ARG, "bins not set up or null capacity");
-    const size_t bytes = (size_t)r->nbx * r->nby * sizeof(uint32_t);
-    GBR_CUDA(cudaMemcpyAsync(r->d_capacity, capacity, bytes, is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                             (cudaStream_t)stream));
+gbr_status gbr_set_raster_params(gbr_renderer* r, uint32_t phase, uint32_t ctas_per_sm) {
+    if (!r || phase > 4096u || (ctas_per_sm != 0 && (ctas_per_sm < 2 || ctas_per_sm > 6)))
+        return fail(GBR_ERR_INVALID_ARG, "phase %u (0..4096) / ctas_per_sm %u (0, 2..6)", phase, ctas_per_sm);
+    r->raster_phase = phase;
+    r->raster_ctas = ctas_per_sm;
+    if (r->bins_ready) {
+        int bps = 0;
+        GBR_CUDA(raster_configure(r->bw, r->bh, ctas_per_sm, &bps));
+        r->raster_blocks_per_sm = std::max(bps, 1);
+    }
     return GBR_OK;
 }
 
@@ -620,6 +613,27 @@ gbr_status gbr_get_bins(gbr_renderer* r, uint32_t* offsets, uint32_t* ids, uint6
     const uint32_t nb = r->nbx * r->nby;
     std::vector<uint32_t> off(nb + 1u);
     GBR_CUDA(cudaMemcpy(off.data(), r->d_offsets, (nb + 1u) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (r->last_predicted && !r->h_ctl->pred_overflow) {
+        // predicted capacities: bin b holds min(cursor - offset, capacity) entries
+        // from its offset; the tail of each bin's capacity is unused
+        std::vector<uint32_t> cur(nb), cap(nb), out_off(nb + 1u, 0u);
+        GBR_CUDA(cudaMemcpy(cur.data(), r->d_cursors, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        GBR_CUDA(cudaMemcpy(cap.data(), r->d_capacity, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint32_t b = 0; b < nb; ++b) out_off[b + 1] = out_off[b] + std::min(cur[b] - off[b], cap[b]);
+        const uint64_t total = out_off[nb];
+        if (num_pairs) *num_pairs = total;
+        if (offsets) memcpy(offsets, out_off.data(), (nb + 1u) * sizeof(uint32_t));
+        if (ids) {
+            if (capacity < total) return fail(GBR_ERR_INVALID_ARG, "ids capacity %llu < %llu pairs",
+                                              (unsigned long long)capacity, (unsigned long long)total);
+            std::vector<uint32_t> all(off[nb]);
+            if (!all.empty())
+                GBR_CUDA(cudaMemcpy(all.data(), r->d_list, all.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            for (uint32_t b = 0; b < nb; ++b)
+                for (uint32_t k = 0; k < out_off[b + 1] - out_off[b]; ++k) ids[out_off[b] + k] = all[off[b] + k] & ~kNoRasterBit;
+        }
+        return GBR_OK;
+    }
     const uint64_t total = off[nb];
     if (num_pairs) *num_pairs = total;
     if (offsets) memcpy(offsets, off.data(), (nb + 1u) * sizeof(uint32_t));
@@ -629,6 +643,59 @@ gbr_status gbr_get_bins(gbr_renderer* r, uint32_t* offsets, uint32_t* ids, uint6
         if (total) GBR_CUDA(cudaMemcpy(ids, r->d_list, total * sizeof(uint32_t), cudaMemcpyDeviceToHost));
         for (uint64_t i = 0; i < total; ++i) ids[i] &= ~kNoRasterBit;
     }
+    return GBR_OK;
+}
+
+gbr_status gbr_set_predictor(gbr_renderer* r, const uint16_t* weights_bf16, uint32_t num_params, float alpha,
+                             float beta, float gamma) {
+    if (!r || !weights_bf16 || num_params != (uint32_t)kMlpParams)
+        return fail(GBR_ERR_INVALID_ARG, "predictor needs %d BF16 parameters", kMlpParams);
+    if (!r->d_mlp_w) GBR_CUDA(cudaMalloc(&r->d_mlp_w, kMlpParamsPadded * sizeof(uint16_t)));
+    GBR_CUDA(cudaMemcpy(r->d_mlp_w, weights_bf16, kMlpParams * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    r->cap_alpha = alpha;
+    r->cap_beta = beta;
+    r->cap_gamma = gamma;
+    r->predictor_ready = true;
+    return GBR_OK;
+}
+
+gbr_status gbr_collect_bin_features(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, uint32_t sample,
+                                    uint32_t vis, float* features, uint32_t* counts, void* stream) {
+    if (!r || !cam || !features || !counts) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    if (!r->bins_ready) return fail(GBR_ERR_INVALID_ARG, "gbr_setup_bins was not called");
+    cudaStream_t s = (cudaStream_t)stream;
+    r->collect = true;
+    gbr_status st = render_frame(r, cam, cull, sample, vis, s);
+    if (st == GBR_OK) st = finish_frame(r, s);
+    r->collect = false;
+    if (st != GBR_OK) return st;
+    const uint32_t nb = r->nbx * r->nby;
+    std::vector<uint32_t> off(nb + 1u);
+    GBR_CUDA(cudaMemcpy(off.data(), r->d_offsets, (nb + 1u) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (uint32_t b = 0; b < nb; ++b) counts[b] = off[b + 1] - off[b];
+    GBR_CUDA(cudaMemcpy(features, r->d_features_out, (size_t)nb * kFeatures * sizeof(float), cudaMemcpyDeviceToHost));
+    return GBR_OK;
+}
+
+uint32_t gbr_mlp_num_params(void) { return (uint32_t)kMlpParams; }
+
+gbr_status gbr_mlp_predict(const uint16_t* d_w, const float* d_x, uint32_t n, float* d_out, void* stream) {
+    if (!d_w || (!d_x && n) || (!d_out && n)) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    GBR_CUDA(launch_mlp_predict(d_w, d_x, n, d_out, (cudaStream_t)stream));
+    return GBR_OK;
+}
+
+gbr_status gbr_mlp_loss_grad(const uint16_t* d_w, const float* d_x, const float* d_y, uint32_t n, float* d_grad,
+                             float* d_loss, void* stream) {
+    if (!d_w || !d_grad || !d_loss || ((!d_x || !d_y) && n)) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    GBR_CUDA(launch_mlp_grad(d_w, d_x, d_y, n, d_grad, d_loss, (cudaStream_t)stream));
+    return GBR_OK;
+}
+
+gbr_status gbr_mlp_adam(float* d_master, uint16_t* d_w, const float* d_grad, float* d_m, float* d_v, uint32_t step,
+                        float lr, float grad_scale, void* stream) {
+    if (!d_master || !d_w || !d_grad || !d_m || !d_v || step == 0) return fail(GBR_ERR_INVALID_ARG, "bad argument");
+    GBR_CUDA(launch_mlp_adam(d_master, d_w, d_grad, d_m, d_v, step, lr, grad_scale, (cudaStream_t)stream));
     return GBR_OK;
 }
 

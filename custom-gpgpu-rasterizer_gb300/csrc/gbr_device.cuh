@@ -23,7 +23,8 @@ constexpr uint32_t kFlagFloat = 2u;               // outside the guard band: flo
 constexpr int kMaxBinDim = 64;
 constexpr int kRasterThreads = 256;
 constexpr int kBatch = 256;
-constexpr uint32_t kPhase = 64;                   // triangles between hierarchical-z refreshes
+constexpr uint32_t kPhase = 16;                   // triangles between hierarchical-z refreshes
+constexpr uint32_t kDefaultRasterCtas = 6;        // raster_kernel variant (CTAs per SM) used by default
 
 enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
 
@@ -73,7 +74,8 @@ struct Ctl {
     uint32_t pred_overflow;    // a predicted per-bin capacity was exceeded
     unsigned long long pred_capacity;
     uint32_t error;            // non-zero: a bounded wait gave up
-    uint32_t pad[5];
+    uint32_t num_sampled;      // visible triangles seen by the coarse pre-pass
+    uint32_t pad[4];
 };
 
 // Everything a kernel of the frame needs, passed by value.
@@ -83,6 +85,8 @@ struct FrameDev {
     uint32_t cull, sample, vis, clear_colour32;
     uint32_t num_meshes, num_tris;
     uint32_t chunk;
+    uint32_t phase;           // triangles between hierarchical-z refreshes (0: kPhase)
+    uint32_t raster_ctas;     // raster_kernel variant: CTAs per SM it is compiled for (0: default)
     float cam_pos[3];
     float cam_fwd[3];
     const MeshDev* meshes;
@@ -102,7 +106,48 @@ struct FrameDev {
     uint32_t* ids;
     unsigned long long* gvis;
     Ctl* ctl;
+    // predicted-capacity binning
+    uint32_t* feat;            // coarse pre-pass accumulators, kFeatSlots x num_bins (slot-major)
+    const uint16_t* mlp_w;     // capacity model parameters, BF16
+    float* features_out;       // optional: kFeatures features per bin (training data)
+    float cap_alpha, cap_beta, cap_gamma;  // capacity = ceil(l*(1+alpha) + beta*sqrt(l) + gamma)
+    uint32_t sample_stride;    // the pre-pass samples every sample_stride-th triangle
+    uint32_t exact_guard;      // exact-binning kernels run only after a predicted overflow
 };
+static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
+
+// Many scenes rendered as one batch frame.  Each scene keeps its own frame
+// descriptor (its resolution, bins, meshes, frame buffers, statistics
+// block); bin counters, setup records and the bin list are slices of
+// batch-wide arrays, and the raster work items of all scenes share one
+// queue.  The block tables map a grid's blocks to scenes: scene s owns
+// blocks [tri_blocks[s], tri_blocks[s+1]) of the setup and fill grids and
+// [px_blocks[s], px_blocks[s+1]) of the shade grid; its bins are global
+// bins [bin_base[s], bin_base[s+1]).
+struct BatchDev {
+    const FrameDev* scenes;
+    const uint32_t* tri_blocks;   // num_scenes + 1
+    const uint32_t* px_blocks;    // num_scenes + 1
+    const uint32_t* bin_base;     // num_scenes + 1
+    uint4* items;                 // (global bin, list start, count, chunks of the bin)
+    Ctl* ctl;                     // the batch's list/item allocation, work queue and overflow flag
+    unsigned long long list_cap;
+    uint32_t items_cap;
+    uint32_t num_scenes;
+    uint32_t phase;               // raster: triangles between hierarchical-z refreshes (0: kPhase)
+    uint32_t pad;
+};
+
+// Index s of the last entry with table[s] <= v among table[0..n) (table
+// non-decreasing, table[0] <= v).
+__device__ __forceinline__ uint32_t scene_of(const uint32_t* table, uint32_t n, uint32_t v) {
+    uint32_t lo = 0, hi = n - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (__ldg(table + mid) <= v) lo = mid; else hi = mid - 1u;
+    }
+    return lo;
+}
 
 // ---------------------------------------------------------------------------
 // Conversions with the semantics of nvcc's cvt.rzi (saturating, NaN -> 0),

@@ -16,6 +16,8 @@
 // Reference stages replaced: VS_Kernel, TA_Kernel, TB_Kernel,
 // RA_PerTileKernel, PS_Kernel and the CLEAR_* kernels
 // (CustomCUDARasterizer/CUDARenderer.cu:598-1129, launchers :1625-1966).
+#include <cstring>
+
 #include "gbr_device.cuh"
 #include "gbr_kernels.h"
 #include "gbr_shade.cuh"
@@ -71,9 +73,11 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
     }
 }
 
+// Vertex stage (positions), triangle assembly, cull, frustum reject, raster
+// setup record and bin rectangle of triangle `prim`, then the count pass
+// (MODE 0) or the predicted-capacity fill (MODE 1).  Called by whole warps.
 template <int MODE>
-__global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
-    const uint32_t prim = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim) {
     const bool in_range = prim < F.num_tris;
     uint2 rect = empty_rect();
     bool visible = false, fpath = false, no_raster = true;
@@ -151,6 +155,14 @@ __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
     else bin_walk<2>(F, rect, prim | (no_raster ? kNoRasterBit : 0u), visible);
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
+    // predicted binning: the exact pass only runs after an overflow, and the
+    // predicted pass stops once an overflow is known
+    if (MODE == 0 ? (F.exact_guard && !F.ctl->pred_overflow) : (F.ctl->pred_overflow != 0u)) return;
+    setup_tri<MODE>(F, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // Single CTA.  counts -> offsets (exclusive, num_bins + 1), cursors, work
 // items; zeroes counts for the next frame.  predicted: capacities replace
 // counts for the offsets, and items are built later by pred_items.
@@ -158,6 +170,7 @@ template <bool PREDICTED>
 __global__ void __launch_bounds__(1024) scan_kernel(FrameDev F) {
     __shared__ uint32_t s_a[1024];
     __shared__ uint32_t s_b[1024];
+    if (!PREDICTED && F.exact_guard && !F.ctl->pred_overflow) return;
     const uint32_t nb = F.num_bins;
     const uint32_t per = (nb + blockDim.x - 1u) / blockDim.x;
     const uint32_t b0 = threadIdx.x * per;
@@ -214,13 +227,17 @@ __global__ void __launch_bounds__(1024) scan_kernel(FrameDev F) {
     }
 }
 
-__global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
-    if (F.ctl->overflow) return;
-    const uint32_t prim = blockIdx.x * blockDim.x + threadIdx.x;
+// Second pass of exact binning for triangle `prim`.  Called by whole warps.
+__device__ __forceinline__ void fill_tri(const FrameDev& F, uint32_t prim) {
     const bool in_range = prim < F.num_tris;
     const uint2 rect = in_range ? F.rects[prim] : empty_rect();
     const uint32_t entry = prim | ((rect.y & 0x80000000u) ? kNoRasterBit : 0u);
     bin_walk<1>(F, rect, entry, in_range);
+}
+
+__global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
+    if (F.ctl->overflow || (F.exact_guard && !F.ctl->pred_overflow)) return;
+    fill_tri(F, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -236,6 +253,13 @@ struct RasterShared {
     int nv;
     int last;
     uint32_t tile_max;   // max depth key over the tile's pixels (0xFFFFFFFF while any pixel is empty)
+    uint32_t key[kBatch];        // depth-key lower bound of each staged triangle
+    uint16_t order[kBatch];      // staged triangles, front to back by 16 key buckets
+    uint32_t bcount[16];
+    uint32_t bstart[17];         // after the scatter: bstart[b] = end of bucket b
+    uint32_t scene_next;         // batch: scene of the fetched work item
+    uint32_t scene_loaded;       // batch: scene whose descriptor `frame` holds
+    __align__(16) FrameDev frame;
 };
 
 // Lower bound of the depth keys any fragment of the triangle can produce.
@@ -248,23 +272,24 @@ struct RasterShared {
 // 2^-18*D^2)/area, every weight is >= -g and the weights sum to 1 +- g, so
 // z >= zmin*(1-g) - (3g + 2^-22)*max|z_i| when zmin >= 0 (2^-22 covers the
 // rounding of the fused z chain).  The key of that bound never exceeds the
-// key of a fragment of the triangle.
-__device__ __forceinline__ bool hiz_reject(const TriSetup& t, int minx, int maxx, int miny, int maxy,
-                                           uint32_t tile_max) {
-    if (tile_max == 0xFFFFFFFFu) return false;
+// key of a fragment of the triangle, so the triangle cannot win a pixel whose
+// stored key is below it.  0: no bound (float path, vertices behind z = 0);
+// 0x7FFFFFFF: every fragment has z >= 1 and loses everywhere.
+__device__ __forceinline__ uint32_t hiz_key(const TriSetup& t) {
+    if (t.flags & kFlagFloat) return 0u;
     const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
-    if (!(zmin >= 0.f)) return false;
+    if (!(zmin >= 0.f)) return 0u;
     const float zabs = fmaxf(fabsf(t.z0), fmaxf(fabsf(t.z1), fabsf(t.z2)));
-    const float D = (float)((maxx - minx) + (maxy - miny)) * (1.0f / 65536.f) + 1.f;
+    const float D = (max3f(t.x0, t.x1, t.x2) - min3f(t.x0, t.x1, t.x2)) + (max3f(t.y0, t.y1, t.y2) - min3f(t.y0, t.y1, t.y2)) + 1.f;
     const float g = (D * 3.0517578125e-05f + 2.3283064365386963e-10f + D * D * 3.814697265625e-06f) * t.inv_area;
     const float zb = zmin * (1.f - g) - (3.f * g + 2.384185791015625e-07f) * zabs;
-    if (!(zb > 0.f)) return false;
-    if (zb >= 1.f) return true;
-    return (uint32_t)__float2int_rz(__fmul_rn(zb, 2147483648.0f)) > tile_max;
+    if (!(zb > 0.f)) return 0u;
+    if (zb >= 1.f) return 0x7FFFFFFFu;
+    return (uint32_t)__float2int_rz(__fmul_rn(zb, 2147483648.0f));
 }
 
 __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
-                                             int ty0, int tw, int th, uint32_t lane, uint32_t tile_max) {
+                                             int ty0, int tw, int th, uint32_t lane) {
     const int X0 = snap_fx(t.x0), Y0 = snap_fx(t.y0), X1 = snap_fx(t.x1);
     const int Y1 = snap_fx(t.y1), X2 = snap_fx(t.x2), Y2 = snap_fx(t.y2);
     const int minx = min(X0, min(X1, X2)), maxx = max(X0, max(X1, X2));
@@ -273,7 +298,6 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
     const int px0 = max((minx + 0xFFFF) >> kFxBits, tx0), px1 = min(maxx >> kFxBits, tx0 + tw - 1);
     const int py0 = max((miny + 0xFFFF) >> kFxBits, ty0), py1 = min(maxy >> kFxBits, ty0 + th - 1);
     if (px0 > px1 || py0 > py1) return;
-    if (hiz_reject(t, minx, maxx, miny, maxy, tile_max)) return;
     const int bwid = px1 - px0 + 1;
     const int lsw = bwid <= 1 ? 0 : bwid <= 2 ? 1 : bwid <= 4 ? 2 : bwid <= 8 ? 3 : bwid <= 16 ? 4 : 5;
     const int sw = 1 << lsw, sh = 32 >> lsw;
@@ -359,31 +383,60 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& F, int x, int y, u
     F.ids[gi] = prim;
 }
 
-__global__ void __launch_bounds__(kRasterThreads, 2) raster_kernel(FrameDev F) {
+// Persistent raster.  Single frame (BATCH false): work items of F.  Batch
+// (BATCH true): work items of all scenes of B; the scene of an item is
+// found from its global bin, and its frame descriptor is copied to shared
+// memory when it differs from the previous item's.
+template <int MIN_CTAS, bool BATCH>
+__global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameDev F, BatchDev B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RasterShared& S = *reinterpret_cast<RasterShared*>(smem_raw);
     unsigned long long* tile = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(RasterShared));
-    if (F.ctl->overflow) return;
+    Ctl* const Q = BATCH ? B.ctl : F.ctl;
+    const uint4* const items = BATCH ? B.items : F.items;
+    if (Q->overflow) return;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t num_items = F.ctl->num_items;
+    const uint32_t num_items = Q->num_items;
+    const uint32_t phase = (BATCH ? B.phase : F.phase) ? (BATCH ? B.phase : F.phase) : kPhase;
+    if (BATCH && tid == 0) S.scene_loaded = 0xFFFFFFFFu;
     for (;;) {
         if (tid == 0) {
-            const uint32_t idx = atomicAdd(&F.ctl->item_next, 1u);
-            const uint4 it = idx < num_items ? F.items[idx] : make_uint4(0xFFFFFFFFu, 0u, 0u, 0u);
+            const uint32_t idx = atomicAdd(&Q->item_next, 1u);
+            uint4 it = idx < num_items ? items[idx] : make_uint4(0xFFFFFFFFu, 0u, 0u, 0u);
+            if (BATCH && it.x != 0xFFFFFFFFu) {
+                const uint32_t sc = scene_of(B.bin_base, B.num_scenes, it.x);
+                S.scene_next = sc;
+                it.x -= __ldg(B.bin_base + sc);
+            }
             S.item[0] = it.x; S.item[1] = it.y; S.item[2] = it.z; S.item[3] = it.w;
         }
         __syncthreads();
         const uint32_t bin = S.item[0];
         if (bin == 0xFFFFFFFFu) break;
+        if (BATCH) {
+            const uint32_t sc = S.scene_next;
+            if (sc != S.scene_loaded) {   // uniform across the CTA
+                const uint4* src = reinterpret_cast<const uint4*>(B.scenes + sc);
+                uint4* dst = reinterpret_cast<uint4*>(&S.frame);
+                for (uint32_t i = tid; i < sizeof(FrameDev) / 16u; i += kRasterThreads) dst[i] = __ldg(src + i);
+                __syncthreads();
+                if (tid == 0) S.scene_loaded = sc;
+            }
+        }
+        const FrameDev& G = BATCH ? S.frame : F;
         const uint32_t start = S.item[1], count = S.item[2], nchunks = S.item[3];
-        const int tx0 = (int)((bin % F.nbx) * F.bw), ty0 = (int)((bin / F.nbx) * F.bh);
-        const int tw = min((int)F.bw, (int)F.width - tx0), th = min((int)F.bh, (int)F.height - ty0);
+        const int tx0 = (int)((bin % G.nbx) * G.bw), ty0 = (int)((bin / G.nbx) * G.bh);
+        const int tw = min((int)G.bw, (int)G.width - tx0), th = min((int)G.bh, (int)G.height - ty0);
         const int npx = (tw > 0 && th > 0) ? tw * th : 0;
+        const uint32_t* const list = G.list;
+        const TriSetup* const setup = G.setup;
+        unsigned long long* const gvis = G.gvis;
+        const uint32_t width = G.width;
         for (int i = (int)tid; i < npx; i += kRasterThreads) tile[i] = kEmptyVis;
         for (uint32_t b0 = 0; b0 < count && npx > 0; b0 += kBatch) {
             __syncthreads();
             const uint32_t n = min((uint32_t)kBatch, count - b0);
-            const uint32_t e = tid < n ? __ldg(F.list + start + b0 + tid) : kNoRasterBit;
+            const uint32_t e = tid < n ? __ldg(list + start + b0 + tid) : kNoRasterBit;
             const bool keep = !(e & kNoRasterBit);
             const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
             if (lane == 0) S.warp_count[warp] = (uint32_t)__popc(bal);
@@ -398,7 +451,7 @@ __global__ void __launch_bounds__(kRasterThreads, 2) raster_kernel(FrameDev F) {
             }
             if (keep) {
                 const uint32_t pos = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
-                const uint4* rp = reinterpret_cast<const uint4*>(F.setup) + 3u * e;
+                const uint4* rp = reinterpret_cast<const uint4*>(setup) + 3u * e;
                 uint4* dst = reinterpret_cast<uint4*>(&S.rec[pos]);
                 dst[0] = __ldg(rp);
                 dst[1] = __ldg(rp + 1);
@@ -406,10 +459,31 @@ __global__ void __launch_bounds__(kRasterThreads, 2) raster_kernel(FrameDev F) {
                 S.prim[pos] = e;
             }
             __syncthreads();
-            // phases of kPhase triangles; the tile's max depth key is refreshed
-            // between phases for the hierarchical-z test
-            for (uint32_t p0 = 0; p0 < total; p0 += kPhase) {
-                const uint32_t p1 = min(total, p0 + kPhase);
+            // front-to-back order: a counting sort of the staged triangles by
+            // the top 4 bits of their depth-key lower bound
+            if (tid < 16) S.bcount[tid] = 0u;
+            __syncthreads();
+            uint32_t bk = 0;
+            if (tid < total) {
+                const uint32_t kb = hiz_key(S.rec[tid]);
+                S.key[tid] = kb;
+                bk = kb >> 27;
+                atomicAdd(&S.bcount[bk], 1u);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                uint32_t a = 0;
+                for (int b = 0; b < 16; ++b) { S.bstart[b] = a; a += S.bcount[b]; }
+                S.bstart[16] = a;
+            }
+            __syncthreads();
+            if (tid < total) S.order[atomicAdd(&S.bstart[bk], 1u)] = (uint16_t)tid;
+            __syncthreads();
+            // phases of `phase` triangles; the tile's max depth key is refreshed
+            // between phases.  A triangle whose key bound exceeds it cannot win
+            // a pixel; once a whole bucket's lower bound does, the rest of the
+            // batch is skipped.
+            for (uint32_t p0 = 0; p0 < total; p0 += phase) {
                 if (b0 > 0 || p0 > 0) {
                     uint32_t m = 0;
                     for (int i = (int)tid; i < npx; i += kRasterThreads)
@@ -425,46 +499,53 @@ __global__ void __launch_bounds__(kRasterThreads, 2) raster_kernel(FrameDev F) {
 #pragma unroll
                     for (uint32_t w = 0; w < kRasterThreads / 32; ++w) tile_max = max(tile_max, S.warp_max[w]);
                 }
+                // buckets [0, tile_max >> 27] can still hold a winner
+                const uint32_t limit = tile_max >= 0x80000000u ? total : S.bstart[tile_max >> 27];
+                if (p0 >= limit) break;   // uniform: every thread sees the same tile_max
+                const uint32_t p1 = min(limit, p0 + phase);
                 for (;;) {
-                    int i = 0;
-                    if (lane == 0) i = atomicAdd(&S.next, 1);
-                    i = __shfl_sync(0xFFFFFFFFu, i, 0);
-                    if (i >= (int)p1) break;
+                    int k = 0;
+                    if (lane == 0) k = atomicAdd(&S.next, 1);
+                    k = __shfl_sync(0xFFFFFFFFu, k, 0);
+                    if (k >= (int)p1) break;
+                    const uint32_t i = S.order[k];
+                    if (S.key[i] > tile_max) continue;
                     const TriSetup& t = S.rec[i];
                     if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
-                    else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane, tile_max);
+                    else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
                 }
                 __syncthreads();
             }
         }
         __syncthreads();
-        if (npx > 0) {
-            if (nchunks == 1u) {
-                for (int i = (int)tid; i < npx; i += kRasterThreads)
-                    resolve_pixel(F, tx0 + i % tw, ty0 + i / tw, tile[i]);
-            } else {
-                for (int i = (int)tid; i < npx; i += kRasterThreads) {
-                    const unsigned long long v = tile[i];
-                    if (v != kEmptyVis)
-                        atomicMin(&F.gvis[(size_t)(ty0 + i / tw) * F.width + (size_t)(tx0 + i % tw)], v);
-                }
-                __threadfence();
-                __syncthreads();
-                if (tid == 0) S.last = atomicAdd(&F.bin_done[bin], 1u) == nchunks - 1u;
-                __syncthreads();
-                if (S.last) {
-                    __threadfence();
-                    for (int i = (int)tid; i < npx; i += kRasterThreads) {
-                        const int x = tx0 + i % tw, y = ty0 + i / tw;
-                        const unsigned long long v = atomicExch(&F.gvis[(size_t)y * F.width + (size_t)x], kEmptyVis);
-                        resolve_pixel(F, x, y, v);
-                    }
-                    if (tid == 0) F.bin_done[bin] = 0u;
-                }
+        // publish the tile: one chunk owns its pixels (plain stores); the
+        // chunks of a longer bin merge with 64-bit atomicMin
+        if (npx > 0 && count > 0) {
+            for (int i = (int)tid; i < npx; i += kRasterThreads) {
+                const unsigned long long v = tile[i];
+                unsigned long long* g = &gvis[(size_t)(ty0 + i / tw) * width + (size_t)(tx0 + i % tw)];
+                if (nchunks == 1u) *g = v;
+                else if (v != kEmptyVis) atomicMin(g, v);
             }
         }
         __syncthreads();
     }
+}
+
+// Shades pixel i of the frame: the winner the raster left in the merge
+// buffer (or the clear colour), and leaves the buffer empty for the next
+// frame.
+__device__ __forceinline__ void shade_px(const FrameDev& F, uint32_t i) {
+    const unsigned long long v = F.gvis[i];
+    if (v != kEmptyVis) F.gvis[i] = kEmptyVis;
+    resolve_pixel(F, (int)(i % F.width), (int)(i / F.width), v);
+}
+
+// One thread per pixel.
+__global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.width * F.height || F.ctl->overflow) return;
+    shade_px(F, i);
 }
 
 // Pixels no bin covers (num_bins * bin_dim smaller than the screen).
@@ -475,6 +556,134 @@ __global__ void clear_kernel(FrameDev F) {
         F.depth[i] = 0.f;
         F.ids[i] = kInvalidPrim;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Batched frames: every stage of all scenes of a batch in one launch
+// ---------------------------------------------------------------------------
+static_assert(sizeof(Ctl) % 16 == 0, "control blocks are cleared as 16-byte words");
+
+// Copies scene sc's frame descriptor into shared memory (whole block).
+__device__ __forceinline__ void load_scene(const BatchDev& B, uint32_t sc, FrameDev& dst) {
+    const uint4* src = reinterpret_cast<const uint4*>(B.scenes + sc);
+    uint4* d = reinterpret_cast<uint4*>(&dst);
+    for (uint32_t i = threadIdx.x; i < sizeof(FrameDev) / 16u; i += blockDim.x) d[i] = __ldg(src + i);
+    __syncthreads();
+}
+
+__device__ __forceinline__ void clear_ctl(Ctl* c) {
+    uint4* w = reinterpret_cast<uint4*>(c);
+#pragma unroll
+    for (uint32_t k = 0; k < sizeof(Ctl) / 16u; ++k) w[k] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Clears the batch's control block and every scene's statistics block.
+__global__ void batch_reset_kernel(BatchDev B) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) clear_ctl(B.ctl);
+    if (i < B.num_scenes) clear_ctl(B.scenes[i].ctl);
+}
+
+// Block -> scene, then the scene's descriptor into shared memory.
+__device__ __forceinline__ uint32_t block_scene(const BatchDev& B, const uint32_t* table, FrameDev& sF,
+                                                uint32_t& s_sc) {
+    if (threadIdx.x == 0) s_sc = scene_of(table, B.num_scenes, blockIdx.x);
+    __syncthreads();
+    const uint32_t sc = s_sc;
+    load_scene(B, sc, sF);
+    return sc;
+}
+
+__global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
+    __shared__ __align__(16) FrameDev sF;
+    __shared__ uint32_t s_sc;
+    const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
+    setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x);
+}
+
+// One CTA per scene: the scene's bin counts -> list offsets, fill cursors
+// and work items.  The scene's list range and item range are allocated
+// from the batch's counters; a range past the storage raises the batch's
+// overflow flag (the later stages then do nothing and the host re-renders
+// the batch with larger storage).
+__global__ void __launch_bounds__(1024) batch_scan_kernel(BatchDev B) {
+    __shared__ uint32_t s_a[1024];
+    __shared__ uint32_t s_b[1024];
+    __shared__ __align__(16) FrameDev sF;
+    __shared__ uint32_t s_run, s_item, s_fits;
+    const uint32_t sc = blockIdx.x;
+    load_scene(B, sc, sF);
+    const FrameDev& F = sF;
+    const uint32_t nb = F.num_bins;
+    const uint32_t per = (nb + blockDim.x - 1u) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    const uint32_t b1 = min(b0 + per, nb);
+    const uint32_t chunk = F.chunk;
+    uint32_t sum = 0, items = 0;
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t c = F.counts[b];
+        sum += c;
+        items += c == 0u ? 1u : (c + chunk - 1u) / chunk;
+    }
+    s_a[threadIdx.x] = sum;
+    s_b[threadIdx.x] = items;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+        const uint32_t a = threadIdx.x >= off ? s_a[threadIdx.x - off] : 0u;
+        const uint32_t c = threadIdx.x >= off ? s_b[threadIdx.x - off] : 0u;
+        __syncthreads();
+        s_a[threadIdx.x] += a;
+        s_b[threadIdx.x] += c;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t total = s_a[blockDim.x - 1u];
+        const uint32_t total_items = s_b[blockDim.x - 1u];
+        const unsigned long long run0 = atomicAdd(&B.ctl->num_pairs, (unsigned long long)total);
+        const uint32_t item0 = atomicAdd(&B.ctl->num_items, total_items);
+        const bool fits = run0 + total <= B.list_cap && (unsigned long long)item0 + total_items <= B.items_cap;
+        if (!fits) atomicOr(&B.ctl->overflow, 1u);
+        s_run = fits ? (uint32_t)run0 : 0u;
+        s_item = item0;
+        s_fits = fits ? 1u : 0u;
+        F.ctl->num_pairs = total;
+        F.ctl->num_items = total_items;
+        F.offsets[nb] = s_run + total;
+    }
+    __syncthreads();
+    const bool fits = s_fits != 0u;
+    const uint32_t gbin = __ldg(B.bin_base + sc);
+    uint32_t run = s_run + s_a[threadIdx.x] - sum;
+    uint32_t item = s_item + s_b[threadIdx.x] - items;
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t c = F.counts[b];
+        F.offsets[b] = run;
+        F.cursors[b] = run;
+        F.counts[b] = 0u;
+        const uint32_t n = c == 0u ? 1u : (c + chunk - 1u) / chunk;
+        if (fits)
+            for (uint32_t k = 0; k < n; ++k)
+                B.items[item + k] = make_uint4(gbin + b, run + k * chunk, min(chunk, c - min(c, k * chunk)), n);
+        item += n;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
+    if (B.ctl->overflow) return;
+    __shared__ __align__(16) FrameDev sF;
+    __shared__ uint32_t s_sc;
+    const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
+    fill_tri(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {
+    if (B.ctl->overflow) return;
+    __shared__ __align__(16) FrameDev sF;
+    __shared__ uint32_t s_sc;
+    const uint32_t sc = block_scene(B, B.px_blocks, sF, s_sc);
+    const uint32_t i = (blockIdx.x - __ldg(B.px_blocks + sc)) * 256u + threadIdx.x;
+    if (i < sF.width * sF.height) shade_px(sF, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -505,8 +714,40 @@ cudaError_t launch_fill(const FrameDev& F, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <bool BATCH>
+static cudaError_t launch_raster_variant(const FrameDev& F, const BatchDev& B, uint32_t ctas, uint32_t grid, size_t smem,
+                                         cudaStream_t s) {
+    switch (ctas ? ctas : kDefaultRasterCtas) {
+        case 2: raster_kernel<2, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
+        case 3: raster_kernel<3, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
+        case 5: raster_kernel<5, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
+        case 6: raster_kernel<6, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
+        default: raster_kernel<4, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
-    raster_kernel<<<grid, kRasterThreads, raster_smem_bytes(F.bw, F.bh), s>>>(F);
+    BatchDev none;
+    memset(&none, 0, sizeof none);
+    cudaError_t e = launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
+    if (e != cudaSuccess) return e;
+    const uint32_t npx = F.width * F.height;
+    shade_kernel<<<(npx + 255u) / 256u, 256, 0, s>>>(F);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s) {
+    if (B.num_scenes == 0) return cudaSuccess;
+    batch_reset_kernel<<<(B.num_scenes + 255u) / 256u, 256, 0, s>>>(B);
+    if (L.tri_blocks) batch_setup_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
+    batch_scan_kernel<<<B.num_scenes, 1024, 0, s>>>(B);
+    if (L.tri_blocks) batch_fill_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
+    FrameDev none;
+    memset(&none, 0, sizeof none);
+    cudaError_t e = launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, raster_smem_bytes(L.bin_w, L.bin_h), s);
+    if (e != cudaSuccess) return e;
+    if (L.px_blocks) batch_shade_kernel<<<L.px_blocks, 256, 0, s>>>(B);
     return cudaGetLastError();
 }
 
@@ -515,11 +756,35 @@ cudaError_t launch_clear(const FrameDev& F, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm) {
-    const size_t smem = raster_smem_bytes(bw, bh);
-    cudaError_t e = cudaFuncSetAttribute(raster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int MIN_CTAS, bool BATCH>
+static cudaError_t configure_variant(size_t smem, int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, raster_kernel, kRasterThreads, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, raster_kernel<MIN_CTAS, BATCH>, kRasterThreads, smem);
+}
+
+template <bool BATCH>
+static cudaError_t configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm) {
+    const size_t smem = raster_smem_bytes(bw, bh);
+    switch (ctas ? ctas : kDefaultRasterCtas) {
+        case 2: return configure_variant<2, BATCH>(smem, blocks_per_sm);
+        case 3: return configure_variant<3, BATCH>(smem, blocks_per_sm);
+        case 5: return configure_variant<5, BATCH>(smem, blocks_per_sm);
+        case 6: return configure_variant<6, BATCH>(smem, blocks_per_sm);
+        default: return configure_variant<4, BATCH>(smem, blocks_per_sm);
+    }
+}
+
+cudaError_t raster_configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm) {
+    return configure<false>(bw, bh, ctas, blocks_per_sm);
+}
+
+cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm) {
+    return configure<true>(bw, bh, ctas, blocks_per_sm);
+}
+
+cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm) {
+    return raster_configure(bw, bh, 0u, blocks_per_sm);
 }
 
 }  // namespace gbr

@@ -8,11 +8,25 @@ namespace gbr {
 
 size_t raster_smem_bytes(uint32_t bw, uint32_t bh);
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm);
+// ctas: the raster_kernel variant compiled for 2..6 CTAs per SM (0: default)
+cudaError_t raster_configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
 cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s);
 cudaError_t launch_scan(const FrameDev& F, bool predicted, cudaStream_t s);
 cudaError_t launch_fill(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s);
 cudaError_t launch_clear(const FrameDev& F, cudaStream_t s);
+
+// Grid sizes of a batch frame (see BatchDev).
+struct BatchLaunch {
+    uint32_t tri_blocks;    // setup / fill blocks of all scenes
+    uint32_t px_blocks;     // shade blocks of all scenes
+    uint32_t raster_grid;   // persistent raster CTAs
+    uint32_t raster_ctas;   // raster variant (CTAs per SM it is compiled for; 0: default)
+    uint32_t bin_w, bin_h;  // the largest bin of the batch (shared-memory tile)
+};
+// reset, setup + count, per-scene scan, fill, raster, shade: six launches
+cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s);
+cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
 
 // Message returned by gbr_last_error_string() on the calling thread.
 void set_last_error(const char* msg);

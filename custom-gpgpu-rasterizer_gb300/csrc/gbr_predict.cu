@@ -1,0 +1,447 @@
+// gbr_predict.cu -- learned per-bin capacity for single-pass binning.
+//
+// Exact binning reads every triangle twice (count pass, then fill pass) with
+// one global atomic per (triangle, bin) pair in each.  Predicted binning
+// replaces the count pass:
+//   prepass_kernel   every sample_stride-th triangle goes through the vertex
+//                    stage and binning rule; per bin it accumulates the
+//                    sampled pair count, and per centroid bin the count,
+//                    bounding-box area (sum, max) and depth range;
+//   capacity_kernel  12 features per bin from those accumulators -> MLP
+//                    12-64-64-1 (ReLU, softplus out; parameters BF16, math
+//                    FP32) -> predicted count l -> capacity
+//                    ceil(l*(1+alpha) + beta*sqrt(l) + gamma);
+//   scan (capacities) -> one fused setup + fill pass appending inside each
+//                    bin's capacity -> items_kernel builds the raster work
+//                    items from the actual counts.
+// Any append beyond a bin's capacity raises ctl->pred_overflow; the exact
+// count / scan / fill kernels are always launched behind it and run only
+// then, so an overflowing frame is re-binned exactly on the device with no
+// host round trip and its bin lists are identical to exact binning's.
+//
+// Training kernels (predict, loss + gradient, Adam) work on (features,
+// exact count) pairs produced by exact binning; the loss is
+// (log1p(l) - log1p(count))^2.
+#include <cuda_bf16.h>
+
+#include "gbr_device.cuh"
+#include "gbr_kernels.h"
+#include "gbr_predict.h"
+
+namespace gbr {
+
+namespace {
+
+__device__ __forceinline__ uint32_t ordered(float f) {
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float unordered(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+__device__ __forceinline__ float bf16_to_f32(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+
+__device__ __forceinline__ uint32_t mesh_of(const FrameDev& F, uint32_t prim) {
+    uint32_t lo = 0, hi = F.num_meshes - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (__ldg(&F.meshes[mid].prim_base) <= prim) lo = mid; else hi = mid - 1u;
+    }
+    return lo;
+}
+
+// Loads the BF16 parameters into shared memory as floats.
+__device__ __forceinline__ void load_params(const uint16_t* w, float* s) {
+    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) s[i] = bf16_to_f32(w[i]);
+    __syncthreads();
+}
+
+// Hidden layer 1 and the pre-softplus output; h1 is kept for the backward pass.
+__device__ __forceinline__ float mlp_forward(const float* w, const float* x, float* h1) {
+#pragma unroll 4
+    for (int j = 0; j < kMlpHidden; ++j) {
+        float a = w[kOffB1 + j];
+#pragma unroll
+        for (int k = 0; k < kFeatures; ++k) a = __fmaf_rn(x[k], w[kOffW1 + k * kMlpHidden + j], a);
+        h1[j] = fmaxf(a, 0.f);
+    }
+    float y = w[kOffB3];
+    for (int j = 0; j < kMlpHidden; ++j) {
+        float a = w[kOffB2 + j];
+#pragma unroll 8
+        for (int i = 0; i < kMlpHidden; ++i) a = __fmaf_rn(h1[i], w[kOffW2 + i * kMlpHidden + j], a);
+        y = __fmaf_rn(fmaxf(a, 0.f), w[kOffW3 + j], y);
+    }
+    return y;
+}
+
+__device__ __forceinline__ float softplus(float y) { return y > 20.f ? y : log1pf(expf(y)); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Frame kernels
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) prepass_kernel(FrameDev F) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t prim = idx * F.sample_stride;
+    const uint32_t lane = threadIdx.x & 31u;
+    bool visible = false;
+    int4 r = make_int4(1, 1, 0, 0);
+    uint32_t cbin = 0;
+    float area = 0.f, zc = 0.f;
+    if (prim < F.num_tris) {
+        const MeshDev& m = F.meshes[mesh_of(F, prim)];
+        uint32_t vid[3];
+        tri_vertex_ids(m, prim - m.prim_base, vid);
+        float nx[3], ny[3], nz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const F3 p = fetch_position(m, vid[k]);
+            const float4 c = xform_point(m.wvp, p.x, p.y, p.z);
+            nx[k] = __fdiv_rn(c.x, c.w);
+            ny[k] = __fdiv_rn(c.y, c.w);
+            nz[k] = __fdiv_rn(c.z, c.w);
+        }
+        bool culled = false;
+        if (F.cull != 2u) {
+            const F3 a = f3(__fsub_rn(nx[1], nx[0]), __fsub_rn(ny[1], ny[0]), __fsub_rn(nz[1], nz[0]));
+            const F3 b = f3(__fsub_rn(nx[2], nx[0]), __fsub_rn(ny[2], ny[0]), __fsub_rn(nz[2], nz[0]));
+            culled = dot3(f3(F.cam_fwd[0], F.cam_fwd[1], F.cam_fwd[2]), normalize3(cross3(a, b))) <= 0.0f;
+        }
+        const bool ax = (nx[0] < -1.f && nx[1] < -1.f && nx[2] < -1.f) || (nx[0] > 1.f && nx[1] > 1.f && nx[2] > 1.f);
+        const bool ay = (ny[0] < -1.f && ny[1] < -1.f && ny[2] < -1.f) || (ny[0] > 1.f && ny[1] > 1.f && ny[2] > 1.f);
+        const bool az = (nz[0] < 0.f && nz[1] < 0.f && nz[2] < 0.f) || (nz[0] > 1.f && nz[1] > 1.f && nz[2] > 1.f);
+        visible = !culled && !ax && !ay && !az;
+        if (visible) {
+            const float2 s0 = to_screen(nx[0], ny[0], F.width, F.height);
+            const float2 s1 = to_screen(nx[1], ny[1], F.width, F.height);
+            const float2 s2 = to_screen(nx[2], ny[2], F.width, F.height);
+            r = bin_rect(s0, s1, s2, F);
+            const float cx = (s0.x + s1.x + s2.x) * (1.f / 3.f), cy = (s0.y + s1.y + s2.y) * (1.f / 3.f);
+            const int bx = clampi((int)floorf(cx / (float)F.bw), 0, (int)F.nbx - 1);
+            const int by = clampi((int)floorf(cy / (float)F.bh), 0, (int)F.nby - 1);
+            cbin = (uint32_t)bx + (uint32_t)by * F.nbx;
+            area = (max3f(s0.x, s1.x, s2.x) - min3f(s0.x, s1.x, s2.x)) * (max3f(s0.y, s1.y, s2.y) - min3f(s0.y, s1.y, s2.y));
+            zc = (nz[0] + nz[1] + nz[2]) * (1.f / 3.f);
+            if (!(area == area) || area > 1e12f) area = 1e12f;
+            if (!(zc == zc)) zc = 0.f;
+        }
+    }
+    const unsigned vis = __ballot_sync(0xFFFFFFFFu, visible);
+    if (lane == 0 && vis) atomicAdd(&F.ctl->num_sampled, (uint32_t)__popc(vis));
+    const uint32_t nb = F.num_bins;
+    if (visible) {
+        atomicAdd(&F.feat[1u * nb + cbin], 1u);
+        atomicAdd(reinterpret_cast<float*>(&F.feat[2u * nb + cbin]), area);
+        atomicMax(&F.feat[3u * nb + cbin], __float_as_uint(area));
+        atomicMin(&F.feat[4u * nb + cbin], ordered(zc));
+        atomicMax(&F.feat[5u * nb + cbin], ordered(zc));
+    }
+    // sampled (triangle, bin) pairs, warp-aggregated
+    bool more = visible && r.x <= r.z && r.y <= r.w;
+    int bx = r.x, by = r.y;
+    for (;;) {
+        const unsigned act = __ballot_sync(0xFFFFFFFFu, more);
+        if (!act) break;
+        if (more) {
+            const uint32_t bin = (uint32_t)bx + (uint32_t)by * F.nbx;
+            const unsigned peers = __match_any_sync(act, bin);
+            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&F.feat[bin], (uint32_t)__popc(peers));
+            if (++bx > r.z) { bx = r.x; if (++by > r.w) more = false; }
+        }
+    }
+}
+
+// The kFeatures features of bin b (shared by inference and training data).
+__device__ __forceinline__ void bin_features(const FrameDev& F, uint32_t b, float* x) {
+    const uint32_t nb = F.num_bins;
+    const float s = (float)F.sample_stride;
+    const int bx = (int)(b % F.nbx), by = (int)(b / F.nbx);
+    auto sc = [&](int x_, int y_) -> float {
+        if (x_ < 0 || y_ < 0 || x_ >= (int)F.nbx || y_ >= (int)F.nby) return 0.f;
+        return (float)__ldg(&F.feat[(uint32_t)x_ + (uint32_t)y_ * F.nbx]) * s;
+    };
+    float n9 = 0.f;
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) n9 += sc(bx + dx, by + dy);
+    const uint32_t cc = __ldg(&F.feat[1u * nb + b]);
+    const float area_sum = __uint_as_float(__ldg(&F.feat[2u * nb + b]));
+    const float area_max = __uint_as_float(__ldg(&F.feat[3u * nb + b]));
+    const int tw = min((int)F.bw, (int)F.width - bx * (int)F.bw), th = min((int)F.bh, (int)F.height - by * (int)F.bh);
+    x[0] = log1pf(sc(bx, by));
+    x[1] = log1pf(n9 * (1.f / 9.f));
+    x[2] = log1pf((float)cc * s);
+    x[3] = cc ? log1pf(area_sum / (float)cc) : 0.f;
+    x[4] = cc ? log1pf(area_max) : 0.f;
+    x[5] = cc ? unordered(__ldg(&F.feat[5u * nb + b])) - unordered(__ldg(&F.feat[4u * nb + b])) : 0.f;
+    x[6] = log1pf(sc(bx - 1, by));
+    x[7] = log1pf(sc(bx + 1, by));
+    x[8] = log1pf(sc(bx, by - 1));
+    x[9] = log1pf(sc(bx, by + 1));
+    x[10] = (tw > 0 && th > 0) ? (float)(tw * th) / (float)(F.bw * F.bh) : 0.f;
+    x[11] = log1pf((float)F.ctl->num_sampled * s / (float)nb);
+}
+
+__global__ void __launch_bounds__(256) capacity_kernel(FrameDev F, int predict) {
+    __shared__ float w[kMlpParams];
+    if (predict) load_params(F.mlp_w, w);
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= F.num_bins) return;
+    float x[kFeatures];
+    bin_features(F, b, x);
+    if (F.features_out)
+        for (int k = 0; k < kFeatures; ++k) F.features_out[(size_t)b * kFeatures + k] = x[k];
+    if (!predict) return;
+    float h1[kMlpHidden];
+    const float l = softplus(mlp_forward(w, x, h1));
+    const float cap = ceilf(l * (1.f + F.cap_alpha) + F.cap_beta * sqrtf(l) + F.cap_gamma);
+    F.capacity[b] = cap >= 4.0e9f ? 0xFFFFFFFFu : (uint32_t)fmaxf(cap, 0.f);
+}
+
+// After the fused setup + fill: work items from the actual per-bin counts,
+// and the pre-pass accumulators reset for the next frame.  On overflow the
+// exact kernels that follow take over.
+__global__ void __launch_bounds__(1024) items_kernel(FrameDev F) {
+    __shared__ uint32_t s_a[1024];
+    __shared__ uint32_t s_b[1024];
+    const uint32_t nb = F.num_bins;
+    const uint32_t per = (nb + blockDim.x - 1u) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per, b1 = min(b0 + per, nb);
+    for (uint32_t b = b0; b < b1; ++b) {
+        F.feat[b] = 0u;
+        F.feat[1u * nb + b] = 0u;
+        F.feat[2u * nb + b] = 0u;
+        F.feat[3u * nb + b] = 0u;
+        F.feat[4u * nb + b] = 0xFFFFFFFFu;
+        F.feat[5u * nb + b] = 0u;
+    }
+    if (F.ctl->pred_overflow) {
+        if (threadIdx.x == 0) {
+            F.ctl->num_visible = 0u;   // the exact pass counts again
+            F.ctl->num_float_path = 0u;
+        }
+        return;
+    }
+    const uint32_t chunk = F.chunk;
+    uint32_t sum = 0, items = 0;
+    for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t c = min(F.cursors[b] - F.offsets[b], F.capacity[b]);
+        sum += c;
+        items += c == 0u ? 1u : (c + chunk - 1u) / chunk;
+    }
+    s_a[threadIdx.x] = sum;
+    s_b[threadIdx.x] = items;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+        const uint32_t a = threadIdx.x >= off ? s_a[threadIdx.x - off] : 0u;
+        const uint32_t c = threadIdx.x >= off ? s_b[threadIdx.x - off] : 0u;
+        __syncthreads();
+        s_a[threadIdx.x] += a;
+        s_b[threadIdx.x] += c;
+        __syncthreads();
+    }
+    uint32_t item = s_b[threadIdx.x] - items;
+    const uint32_t total_items = s_b[blockDim.x - 1u];
+    const bool fits = total_items <= F.items_cap;
+    for (uint32_t b = b0; b < b1 && fits; ++b) {
+        const uint32_t c = min(F.cursors[b] - F.offsets[b], F.capacity[b]);
+        const uint32_t n = c == 0u ? 1u : (c + chunk - 1u) / chunk;
+        for (uint32_t k = 0; k < n; ++k)
+            F.items[item + k] = make_uint4(b, F.offsets[b] + k * chunk, min(chunk, c - min(c, k * chunk)), n);
+        item += n;
+    }
+    if (threadIdx.x == 0) {
+        F.ctl->num_pairs = s_a[blockDim.x - 1u];
+        F.ctl->num_items = fits ? total_items : 0u;
+        F.ctl->item_next = 0u;
+        if (!fits) F.ctl->pred_overflow = 1u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training kernels
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) mlp_predict_kernel(const uint16_t* wq, const float* x, uint32_t n, float* out) {
+    __shared__ float w[kMlpParams];
+    load_params(wq, w);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float h1[kMlpHidden];
+    out[i] = softplus(mlp_forward(w, x + (size_t)i * kFeatures, h1));
+}
+
+// One sample per thread, kGradSamples samples per block; weight gradients
+// are sums over the block's samples, added to `grad` with atomics.
+__global__ void __launch_bounds__(kGradSamples) mlp_grad_kernel(const uint16_t* wq, const float* x, const float* y,
+                                                              uint32_t n, float* grad, float* loss) {
+    extern __shared__ float sm[];
+    float* w = sm;                                   // kMlpParams
+    float* H1 = w + kMlpParamsPadded;                // [kGradSamples][kMlpHidden]: h1, later dh1
+    float* D2 = H1 + kGradSamples * kMlpHidden;      // [kGradSamples][kMlpHidden]: h2, later dh2
+    float* X = D2 + kGradSamples * kMlpHidden;       // [kGradSamples][kFeatures]
+    float* G = X + kGradSamples * kFeatures;         // [kGradSamples]: dL/d(output pre-softplus)
+    load_params(wq, w);
+    const uint32_t t = threadIdx.x;
+    const uint32_t i = blockIdx.x * kGradSamples + t;
+    const bool valid = i < n;
+    float* h1 = H1 + t * kMlpHidden;
+    float* h2 = D2 + t * kMlpHidden;
+    float* xs = X + t * kFeatures;
+    float g = 0.f, l = 0.f;
+    if (valid) {
+        for (int k = 0; k < kFeatures; ++k) xs[k] = x[(size_t)i * kFeatures + k];
+        for (int j = 0; j < kMlpHidden; ++j) {
+            float a = w[kOffB1 + j];
+            for (int k = 0; k < kFeatures; ++k) a = __fmaf_rn(xs[k], w[kOffW1 + k * kMlpHidden + j], a);
+            h1[j] = fmaxf(a, 0.f);
+        }
+        float out = w[kOffB3];
+        for (int j = 0; j < kMlpHidden; ++j) {
+            float a = w[kOffB2 + j];
+            for (int k = 0; k < kMlpHidden; ++k) a = __fmaf_rn(h1[k], w[kOffW2 + k * kMlpHidden + j], a);
+            h2[j] = fmaxf(a, 0.f);
+            out = __fmaf_rn(h2[j], w[kOffW3 + j], out);
+        }
+        const float lam = softplus(out);
+        const float d = log1pf(lam) - log1pf(y[i]);
+        l = d * d;
+        const float sig = 1.f / (1.f + expf(-out));   // d softplus / d out
+        g = 2.f * d / (1.f + lam) * sig;
+    } else {
+        for (int k = 0; k < kFeatures; ++k) xs[k] = 0.f;
+        for (int j = 0; j < kMlpHidden; ++j) { h1[j] = 0.f; h2[j] = 0.f; }
+    }
+    G[t] = g;
+    // loss sum
+    float ls = l;
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xFFFFFFFFu, ls, o);
+    if ((t & 31u) == 0) atomicAdd(loss, ls);
+    __syncthreads();
+    // output layer: dW3[j] = sum_s g_s h2_s[j], db3 = sum_s g_s
+    for (int j = t; j < kMlpHidden; j += kGradSamples) {
+        float a = 0.f;
+        for (int s = 0; s < kGradSamples; ++s) a = __fmaf_rn(G[s], D2[s * kMlpHidden + j], a);
+        atomicAdd(&grad[kOffW3 + j], a);
+    }
+    if (t == 0) {
+        float a = 0.f;
+        for (int s = 0; s < kGradSamples; ++s) a += G[s];
+        atomicAdd(&grad[kOffB3], a);
+    }
+    __syncthreads();
+    // dh2 = g * W3 * [h2 > 0] (in place)
+    for (int j = 0; j < kMlpHidden; ++j) h2[j] = h2[j] > 0.f ? g * w[kOffW3 + j] : 0.f;
+    __syncthreads();
+    // dW2[k][j] = sum_s h1_s[k] dh2_s[j]; db2[j] = sum_s dh2_s[j]
+    for (int e = t; e < kMlpHidden * kMlpHidden; e += kGradSamples) {
+        const int k = e / kMlpHidden, j = e % kMlpHidden;
+        float a = 0.f;
+        for (int s = 0; s < kGradSamples; ++s) a = __fmaf_rn(H1[s * kMlpHidden + k], D2[s * kMlpHidden + j], a);
+        atomicAdd(&grad[kOffW2 + e], a);
+    }
+    for (int j = t; j < kMlpHidden; j += kGradSamples) {
+        float a = 0.f;
+        for (int s = 0; s < kGradSamples; ++s) a += D2[s * kMlpHidden + j];
+        atomicAdd(&grad[kOffB2 + j], a);
+    }
+    __syncthreads();
+    // dh1 = (W2 dh2) * [h1 > 0] (in place)
+    for (int k = 0; k < kMlpHidden; ++k) {
+        float a = 0.f;
+        for (int j = 0; j < kMlpHidden; ++j) a = __fmaf_rn(w[kOffW2 + k * kMlpHidden + j], h2[j], a);
+        h1[k] = h1[k] > 0.f ? a : 0.f;
+    }
+    __syncthreads();
+    // dW1[k][j] = sum_s x_s[k] dh1_s[j]; db1[j] = sum_s dh1_s[j]
+    for (int e = t; e < kFeatures * kMlpHidden; e += kGradSamples) {
+        const int k = e / kMlpHidden, j = e % kMlpHidden;
+        float a = 0.f;
+        for (int s = 0; s < kGradSamples; ++s) a = __fmaf_rn(X[s * kFeatures + k], H1[s * kMlpHidden + j], a);
+        atomicAdd(&grad[kOffW1 + e], a);
+    }
+    for (int j = t; j < kMlpHidden; j += kGradSamples) {
+        float a = 0.f;
+        for (int s = 0; s < kGradSamples; ++s) a += H1[s * kMlpHidden + j];
+        atomicAdd(&grad[kOffB1 + j], a);
+    }
+}
+
+// Adam on FP32 master parameters; the BF16 copy the kernels read is
+// refreshed from them (round to nearest even).
+__global__ void mlp_adam_kernel(float* master, uint16_t* wq, const float* grad, float* m, float* v, uint32_t step,
+                                float lr, float grad_scale) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)kMlpParams) return;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float g = grad[i] * grad_scale;
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / (1.f - powf(b1, (float)step));
+    const float vh = vi / (1.f - powf(b2, (float)step));
+    const float p = master[i] - lr * mh / (sqrtf(vh) + eps);
+    master[i] = p;
+    wq[i] = __bfloat16_as_ushort(__float2bfloat16_rn(p));
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+cudaError_t launch_prepass(const FrameDev& F, cudaStream_t s) {
+    const uint32_t n = (F.num_tris + F.sample_stride - 1u) / F.sample_stride;
+    if (n) prepass_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(F);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_capacity(const FrameDev& F, bool predict, cudaStream_t s) {
+    capacity_kernel<<<(F.num_bins + 255u) / 256u, 256, 0, s>>>(F, predict ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_items(const FrameDev& F, cudaStream_t s) {
+    items_kernel<<<1, 1024, 0, s>>>(F);
+    return cudaGetLastError();
+}
+
+__global__ void feat_reset_kernel(FrameDev F) {
+    const uint32_t nb = F.num_bins;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        F.feat[b] = 0u;
+        F.feat[1u * nb + b] = 0u;
+        F.feat[2u * nb + b] = 0u;
+        F.feat[3u * nb + b] = 0u;
+        F.feat[4u * nb + b] = 0xFFFFFFFFu;
+        F.feat[5u * nb + b] = 0u;
+    }
+}
+
+cudaError_t launch_feat_reset(const FrameDev& F, cudaStream_t s) {
+    feat_reset_kernel<<<(F.num_bins + 255u) / 256u, 256, 0, s>>>(F);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_predict(const uint16_t* w, const float* x, uint32_t n, float* out, cudaStream_t s) {
+    if (n) mlp_predict_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(w, x, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad(const uint16_t* w, const float* x, const float* y, uint32_t n, float* grad, float* loss,
+                            cudaStream_t s) {
+    const size_t smem = ((size_t)kMlpParamsPadded + 2u * kGradSamples * kMlpHidden + kGradSamples * kFeatures +
+                         kGradSamples) * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (n) mlp_grad_kernel<<<(n + kGradSamples - 1u) / kGradSamples, kGradSamples, smem, s>>>(w, x, y, n, grad, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_adam(float* master, uint16_t* wq, const float* grad, float* m, float* v, uint32_t step, float lr,
+                            float grad_scale, cudaStream_t s) {
+    mlp_adam_kernel<<<(kMlpParams + 255) / 256, 256, 0, s>>>(master, wq, grad, m, v, step, lr, grad_scale);
+    return cudaGetLastError();
+}
+
+}  // namespace gbr

@@ -30,9 +30,13 @@ BINNING_EXACT, BINNING_PREDICTED = 0, 1
 
 EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "gbr_mesh_update_vertices",
             "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
-            "gbr_texture_upload", "gbr_texture_remove", "gbr_set_binning", "gbr_set_bin_capacity",
-            "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
-            "gbr_get_bins", "gbr_get_stats", "gbr_render_noalloc", "gbr_last_error_string", "gbr_version"]
+            "gbr_texture_upload", "gbr_texture_remove", "gbr_set_binning", "gbr_set_predictor",
+            "gbr_collect_bin_features", "gbr_mlp_num_params", "gbr_mlp_predict", "gbr_mlp_loss_grad", "gbr_mlp_adam",
+            "gbr_set_raster_params", "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
+            "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
+            "gbr_batch_set_view", "gbr_batch_set_config", "gbr_batch_get_config", "gbr_batch_autotune",
+            "gbr_batch_set_timing", "gbr_batch_render", "gbr_batch_get_stats", "gbr_batch_scene_bins",
+            "gbr_batch_readback", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_last_error_string", "gbr_version"]
 
 
 class GbrError(RuntimeError):
@@ -51,6 +55,18 @@ class Stats(C.Structure):
                 ("overflow_reruns", C.c_uint32), ("predicted_overflow", C.c_uint32),
                 ("predicted_capacity", C.c_uint64),
                 ("ms_setup", C.c_float), ("ms_bin", C.c_float), ("ms_raster", C.c_float), ("ms_total", C.c_float)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("bin_size", C.c_uint32), ("queue_chunk", C.c_uint32), ("raster_ctas", C.c_uint32),
+                ("raster_phase", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("num_scenes", C.c_uint32), ("graph_captures", C.c_uint32), ("overflow_reruns", C.c_uint32),
+                ("pad", C.c_uint32), ("num_triangles", C.c_uint64), ("num_visible", C.c_uint64),
+                ("num_pairs", C.c_uint64), ("num_work_items", C.c_uint64), ("ms_frame", C.c_float),
+                ("pad2", C.c_float)]
 
 
 _LIB = None
@@ -81,7 +97,12 @@ def lib():
             "gbr_texture_upload": [vp, vp, u32, u32, C.POINTER(i32)],
             "gbr_texture_remove": [vp, i32],
             "gbr_set_binning": [vp, u32],
-            "gbr_set_bin_capacity": [vp, vp, C.c_int, vp],
+            "gbr_set_predictor": [vp, vp, u32, C.c_float, C.c_float, C.c_float],
+            "gbr_collect_bin_features": [vp, C.POINTER(Camera), u32, u32, u32, vp, vp, vp],
+            "gbr_mlp_predict": [vp, vp, u32, vp, vp],
+            "gbr_mlp_loss_grad": [vp, vp, vp, u32, vp, vp, vp],
+            "gbr_mlp_adam": [vp, vp, vp, vp, vp, u32, C.c_float, C.c_float, vp],
+            "gbr_set_raster_params": [vp, u32, u32],
             "gbr_set_timing": [vp, C.c_int],
             "gbr_render": [vp, C.POINTER(Camera), u32, u32, u32, vp],
             "gbr_readback": [vp, vp, vp, vp],
@@ -91,6 +112,19 @@ def lib():
             "gbr_get_stats": [vp, C.POINTER(Stats), vp],
             "gbr_render_noalloc": [vp, u32, u32, vp, u32, u32, vp, C.POINTER(Camera), u32, u32, u32, u32, u32, u32,
                                    u32, u32, u32, u32, vp, vp, vp],
+            "gbr_batch_create": [C.POINTER(vp)],
+            "gbr_batch_destroy": [vp],
+            "gbr_batch_add": [vp, vp, C.POINTER(Camera), u32, u32, u32, C.POINTER(u32)],
+            "gbr_batch_set_view": [vp, u32, C.POINTER(Camera), u32, u32, u32],
+            "gbr_batch_set_config": [vp, C.POINTER(BatchConfig)],
+            "gbr_batch_get_config": [vp, C.POINTER(BatchConfig)],
+            "gbr_batch_autotune": [vp, vp, u32, vp, u32, vp, u32, u32, vp, C.POINTER(BatchConfig)],
+            "gbr_batch_set_timing": [vp, C.c_int],
+            "gbr_batch_render": [vp, vp],
+            "gbr_batch_get_stats": [vp, C.POINTER(BatchStats), vp],
+            "gbr_batch_scene_bins": [vp, u32, C.POINTER(u32), C.POINTER(u32)],
+            "gbr_batch_readback": [vp, u32, vp, vp, vp, vp],
+            "gbr_batch_get_bins": [vp, u32, vp, vp, u64, C.POINTER(u64), vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -100,6 +134,8 @@ def lib():
         L.gbr_last_error_string.argtypes = []
         L.gbr_version.restype = C.c_uint32
         L.gbr_version.argtypes = []
+        L.gbr_mlp_num_params.restype = C.c_uint32
+        L.gbr_mlp_num_params.argtypes = []
         _LIB = L
     return _LIB
 
@@ -209,6 +245,9 @@ class Renderer:
     def set_binning(self, method: int):
         check(self._lib.gbr_set_binning(self.h, method))
 
+    def set_raster_params(self, phase: int = 0, ctas_per_sm: int = 0):
+        check(self._lib.gbr_set_raster_params(self.h, phase, ctas_per_sm))
+
     def set_timing(self, on: bool):
         check(self._lib.gbr_set_timing(self.h, 1 if on else 0))
 
@@ -258,3 +297,113 @@ class Renderer:
         st = Stats()
         check(self._lib.gbr_get_stats(self.h, C.byref(st), C.c_void_p(stream) if stream else None))
         return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+
+def _stream(stream: int):
+    return C.c_void_p(stream) if stream else None
+
+
+def _u32_list(values):
+    if values is None:
+        return None, 0
+    arr = (C.c_uint32 * len(values))(*[int(v) for v in values])
+    return arr, len(values)
+
+
+class Batch:
+    """Many renderers' scenes rendered as one batch frame (gbr_batch_*): one
+    persistent launch chain over the (scene, bin) work items of every scene,
+    replayed from a CUDA graph."""
+
+    def __init__(self):
+        self._lib = lib()
+        h = C.c_void_p()
+        check(self._lib.gbr_batch_create(C.byref(h)))
+        self.h = h
+        self.renderers = []
+
+    def close(self):
+        if self.h:
+            self._lib.gbr_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add(self, renderer: Renderer, camera, cull: int, sample: int, vis: int) -> int:
+        cam = camera if isinstance(camera, Camera) else make_camera(camera)
+        idx = C.c_uint32()
+        check(self._lib.gbr_batch_add(self.h, renderer.h, C.byref(cam), cull, sample, vis, C.byref(idx)))
+        self.renderers.append(renderer)
+        return idx.value
+
+    def add_scene(self, renderer: Renderer, scene) -> int:
+        return self.add(renderer, scene.camera, scene.cull, scene.sample, scene.vis)
+
+    def set_view(self, index: int, camera, cull: int, sample: int, vis: int):
+        cam = camera if isinstance(camera, Camera) else make_camera(camera)
+        check(self._lib.gbr_batch_set_view(self.h, index, C.byref(cam), cull, sample, vis))
+
+    def set_config(self, bin_size: int = 16, queue_chunk: int = 64, raster_ctas: int = 0, raster_phase: int = 0):
+        cfg = BatchConfig(bin_size, queue_chunk, raster_ctas, raster_phase)
+        check(self._lib.gbr_batch_set_config(self.h, C.byref(cfg)))
+
+    def config(self) -> dict:
+        cfg = BatchConfig()
+        check(self._lib.gbr_batch_get_config(self.h, C.byref(cfg)))
+        return {k: getattr(cfg, k) for k, _ in BatchConfig._fields_}
+
+    def autotune(self, bin_sizes=(8, 16, 32), chunks=(32, 64, 128), raster_ctas=None, frames: int = 2,
+                 stream: int = 0) -> dict:
+        b, nb = _u32_list(bin_sizes)
+        c, nc = _u32_list(chunks)
+        r, nr = _u32_list(raster_ctas)
+        best = BatchConfig()
+        check(self._lib.gbr_batch_autotune(self.h, b, nb, c, nc, r, nr, frames, _stream(stream), C.byref(best)))
+        return {k: getattr(best, k) for k, _ in BatchConfig._fields_}
+
+    def set_timing(self, on: bool):
+        check(self._lib.gbr_batch_set_timing(self.h, 1 if on else 0))
+
+    def render(self, stream: int = 0):
+        check(self._lib.gbr_batch_render(self.h, _stream(stream)))
+
+    def stats(self, stream: int = 0) -> dict:
+        st = BatchStats()
+        check(self._lib.gbr_batch_get_stats(self.h, C.byref(st), _stream(stream)))
+        return {k: getattr(st, k) for k, _ in BatchStats._fields_ if not k.startswith("pad")}
+
+    def readback(self, index: int, stream: int = 0):
+        """(colour, depth, ids) of scene `index`, each [height, width]."""
+        r = self.renderers[index]
+        n = r.width * r.height
+        colour = np.empty(n, np.uint32)
+        depth = np.empty(n, np.float32)
+        ids = np.empty(n, np.uint32)
+        check(self._lib.gbr_batch_readback(self.h, index, _ptr(colour), _ptr(depth), _ptr(ids), _stream(stream)))
+        shp = (r.height, r.width)
+        return colour.reshape(shp), depth.reshape(shp), ids.reshape(shp)
+
+    def get_bins(self, index: int, stream: int = 0):
+        """(offsets[num_bins+1], ids) of scene `index`; ids sorted within each bin."""
+        nbx, nby = C.c_uint32(), C.c_uint32()
+        check(self._lib.gbr_batch_scene_bins(self.h, index, C.byref(nbx), C.byref(nby)))
+        nb = nbx.value * nby.value
+        offsets = np.empty(nb + 1, np.uint32)
+        n = C.c_uint64()
+        s = _stream(stream)
+        check(self._lib.gbr_batch_get_bins(self.h, index, _ptr(offsets), None, 0, C.byref(n), s))
+        ids = np.empty(max(n.value, 1), np.uint32)
+        check(self._lib.gbr_batch_get_bins(self.h, index, _ptr(offsets), _ptr(ids), n.value, C.byref(n), s))
+        ids = ids[: n.value]
+        bin_of = np.repeat(np.arange(nb, dtype=np.uint32), np.diff(offsets.astype(np.int64)))
+        return offsets, ids[np.lexsort((ids, bin_of))]

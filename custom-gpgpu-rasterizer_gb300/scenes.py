@@ -237,9 +237,156 @@ def soup_scene(n: int = 1_000_000, width: int = 1920, height: int = 1080, bin_si
                  cull=cull, seed=seed)
 
 
+BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1024, 768), (1920, 1080))
+
+
+def batch_scenes(n: int = 256, seed: int = 0, min_tris: int = 1000, max_tris: int = 500_000,
+                 bin_size: int = 16, resolutions=BATCH_RESOLUTIONS) -> list:
+    """Uneven batch of soups: scene i has a triangle count log-uniform in
+    [min_tris, max_tris] and a resolution drawn from `resolutions`; each is
+    drawn like the 1M soup (uniform centroids plus a 20% Gaussian blob of
+    sigma 100 px, area log-uniform in 0.5-4096 px^2, random winding, depth
+    uniform in [0.1, 100], RGBA8 colours), seeded by (seed, i)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        count = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
+        w, h = resolutions[int(rng.integers(0, len(resolutions)))]
+        s = soup_scene(count, w, h, bin_size, seed=int(rng.integers(1 << 31)))
+        s.name = f"batch{i}_soup{count}_{w}x{h}"
+        out.append(s)
+    return out
+
+
 def pos3_to_ivertex(v: np.ndarray) -> np.ndarray:
     out = np.zeros(len(v), IVERTEX56)
     out["p"] = v["p"]
     rgba = v["rgba"]
     out["c"] = np.stack([(rgba & 0xFF), (rgba >> 8) & 0xFF, (rgba >> 16) & 0xFF], -1).astype(np.float32) / np.float32(255.0)
     return out
+
+
+# ---------------------------------------------------------------------------
+# Dense sub-pixel mesh: displaced icosphere at 4K
+# ---------------------------------------------------------------------------
+def _value_noise_table(seed: int):
+    rng = np.random.default_rng(seed)
+    return rng.permutation(256).astype(np.int64), rng.uniform(-1.0, 1.0, 256)
+
+
+def _fade(t):
+    return t * t * (3.0 - 2.0 * t)
+
+
+def value_noise3(p: np.ndarray, seed: int, octaves: int = 3, base_freq: float = 4.0) -> np.ndarray:
+    """Seeded lattice value noise in [-1, 1] (trilinear, smoothstep fade),
+    `octaves` octaves with doubling frequency and halving amplitude."""
+    perm, vals = _value_noise_table(seed)
+    out = np.zeros(len(p))
+    amp_sum = 0.0
+    for o in range(octaves):
+        f = base_freq * (2 ** o)
+        a = 0.5 ** o
+        q = p * f
+        i0 = np.floor(q).astype(np.int64)
+        t = _fade(q - i0)
+        acc = 0.0
+        for dx in (0, 1):
+            for dy in (0, 1):
+                for dz in (0, 1):
+                    h = perm[(perm[(perm[(i0[:, 0] + dx) & 255] + i0[:, 1] + dy) & 255] + i0[:, 2] + dz) & 255]
+                    w = (t[:, 0] if dx else 1 - t[:, 0]) * (t[:, 1] if dy else 1 - t[:, 1]) * \
+                        (t[:, 2] if dz else 1 - t[:, 2])
+                    acc = acc + w * vals[h]
+        out += a * acc
+        amp_sum += a
+    return out / amp_sum
+
+
+def value_noise2(w: int, h: int, seed: int, octaves: int = 4, base_cells: int = 8) -> np.ndarray:
+    perm, vals = _value_noise_table(seed)
+    ys, xs = np.mgrid[0:h, 0:w]
+    out = np.zeros((h, w))
+    amp_sum = 0.0
+    for o in range(octaves):
+        cells = base_cells * (2 ** o)
+        qx, qy = xs * cells / w, ys * cells / h
+        ix, iy = np.floor(qx).astype(np.int64), np.floor(qy).astype(np.int64)
+        tx, ty = _fade(qx - ix), _fade(qy - iy)
+        acc = 0.0
+        for dx in (0, 1):
+            for dy in (0, 1):
+                hh = perm[(perm[(ix + dx) & 255] + iy + dy) & 255]
+                acc = acc + (tx if dx else 1 - tx) * (ty if dy else 1 - ty) * vals[hh]
+        out += 0.5 ** o * acc
+        amp_sum += 0.5 ** o
+    return out / amp_sum
+
+
+def noise_texture(size: int = 2048, seed: int = 7) -> np.ndarray:
+    n = 0.5 + 0.5 * value_noise2(size, size, seed)
+    r = np.clip(40 + 180 * n, 0, 255).astype(np.uint32)
+    g = np.clip(80 + 150 * n * n, 0, 255).astype(np.uint32)
+    b = np.clip(200 - 150 * n, 0, 255).astype(np.uint32)
+    return r | (g << 8) | (b << 16) | np.uint32(255 << 24)
+
+
+def icosphere_mesh(subdiv: int = 7, amplitude: float = 0.05, seed: int = 3) -> Mesh:
+    """Icosahedron subdivided `subdiv` times (20*4^n triangles, 10*4^n+2
+    vertices), radially displaced by seeded 3-octave value noise of the given
+    amplitude; normals from the displaced surface, spherical UVs."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    F = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                  (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                  (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], np.int64)
+    for _ in range(subdiv):
+        nf = len(F)
+        e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+        uniq, inv = np.unique(np.sort(e, axis=1), axis=0, return_inverse=True)
+        inv = inv.reshape(-1)
+        mid = V[uniq[:, 0]] + V[uniq[:, 1]]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        mid_idx = len(V) + np.arange(len(uniq))
+        V = np.concatenate([V, mid])
+        a, b, c = mid_idx[inv[:nf]], mid_idx[inv[nf:2 * nf]], mid_idx[inv[2 * nf:]]
+        F = np.concatenate([np.stack([F[:, 0], a, c], 1), np.stack([F[:, 1], b, a], 1),
+                            np.stack([F[:, 2], c, b], 1), np.stack([a, b, c], 1)])
+    r = 1.0 + amplitude * value_noise3(V, seed)
+    P = V * r[:, None]
+    fn = np.cross(P[F[:, 1]] - P[F[:, 0]], P[F[:, 2]] - P[F[:, 0]])
+    flip = (fn * P[F].mean(axis=1)).sum(-1) < 0
+    F[flip] = F[flip][:, [0, 2, 1]]
+    fn[flip] = -fn[flip]
+    N = np.zeros_like(P)
+    for k in range(3):
+        np.add.at(N, F[:, k], fn)
+    N /= np.maximum(np.linalg.norm(N, axis=1, keepdims=True), 1e-12)
+    T = np.cross(np.array([0.0, 1.0, 0.0]), N)
+    tl = np.linalg.norm(T, axis=1, keepdims=True)
+    T = np.where(tl > 1e-6, T / np.maximum(tl, 1e-12), np.array([1.0, 0.0, 0.0]))
+    v = np.zeros(len(P), IVERTEX56)
+    v["p"] = P.astype(np.float32)
+    v["n"] = N.astype(np.float32)
+    v["tan"] = T.astype(np.float32)
+    v["uv"] = np.stack([0.5 + np.arctan2(V[:, 2], V[:, 0]) / (2 * math.pi), np.arccos(np.clip(V[:, 1], -1, 1)) / math.pi],
+                       -1).astype(np.float32)
+    v["c"] = 1.0
+    return Mesh(vertices=v, indices=F.reshape(-1).astype(np.uint32))
+
+
+def icosphere_scene(width: int = 3840, height: int = 2160, bin_size: int = 16, subdiv: int = 7,
+                    tex_size: int = 2048, distance: float = 8.0, sample: int = SAMPLE_LINEAR,
+                    vis: int = VIS_PBR) -> Scene:
+    """Displaced icosphere (327,680 triangles at 7 subdivisions) 8 units from
+    a 60 deg camera at 4K, so most triangles cover under 1 px^2; a 2048^2
+    noise texture with the reference's shader (all four maps bound, as the
+    sphere scene) and its "linear" sampler."""
+    mesh = icosphere_mesh(subdiv)
+    mesh.textures = [noise_texture(tex_size), flat_texture(tex_size, (128, 128, 255)),
+                     flat_texture(tex_size, (0, 0, 0)), flat_texture(tex_size, (128, 128, 128))]
+    cam = perspective_camera((0.0, 0.0, distance), 60.0, width, height)
+    return Scene(f"icosphere{subdiv}", width, height, bin_size, bin_size, cam, [mesh], cull=CULL_BACKFACE,
+                 sample=sample, vis=vis)

@@ -119,11 +119,37 @@ gbr_status gbr_texture_upload(gbr_renderer *r, const uint32_t *rgba8, uint32_t w
 /* CUDATextureManager::RemoveCUDATexture (CUDATextureManager.cpp:39-54) */
 gbr_status gbr_texture_remove(gbr_renderer *r, int32_t tex_id);
 
+/* Learned bin capacity (no counterpart in the reference, whose queues have a
+ * fixed size and drop triangles when full, CUDAAtomicQueue.cuh:8-26).
+ * gbr_set_predictor installs the capacity model: num_params BF16 parameters
+ * of the 12-64-64-1 MLP (gbr_mlp_num_params()) and the capacity rule
+ * ceil(l*(1+alpha) + beta*sqrt(l) + gamma) for a predicted count l.  With
+ * GBR_BINNING_PREDICTED a frame bins in one pass into the predicted
+ * capacities; if any bin overflows, the frame is re-binned exactly on the
+ * device, so bin lists and images never depend on the prediction.
+ * gbr_collect_bin_features renders one exact frame and returns, per bin, the
+ * model's 12 input features and the exact triangle count (training data).
+ * gbr_mlp_* are the model's GPU kernels on caller device buffers: forward
+ * predictions, loss + gradient (added into d_grad and d_loss; loss =
+ * (log1p(l) - log1p(count))^2 summed), and one Adam step on FP32 master
+ * parameters that also refreshes their BF16 copy. */
+gbr_status gbr_set_predictor(gbr_renderer *r, const uint16_t *weights_bf16, uint32_t num_params, float alpha,
+                             float beta, float gamma);
+gbr_status gbr_collect_bin_features(gbr_renderer *r, const gbr_camera *cam, uint32_t cull, uint32_t sample,
+                                    uint32_t vis, float *features, uint32_t *counts, void *stream);
+uint32_t gbr_mlp_num_params(void);
+gbr_status gbr_mlp_predict(const uint16_t *d_w, const float *d_x, uint32_t n, float *d_out, void *stream);
+gbr_status gbr_mlp_loss_grad(const uint16_t *d_w, const float *d_x, const float *d_y, uint32_t n, float *d_grad,
+                             float *d_loss, void *stream);
+gbr_status gbr_mlp_adam(float *d_master, uint16_t *d_w, const float *d_grad, float *d_m, float *d_v, uint32_t step,
+                        float lr, float grad_scale, void *stream);
+
 /* Binning method for the following frames. */
 gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
-/* Per-bin capacities for GBR_BINNING_PREDICTED (device or host pointer
- * according to is_device), num_bins_x*num_bins_y entries. */
-gbr_status gbr_set_bin_capacity(gbr_renderer *r, const uint32_t *capacity, int is_device, void *stream);
+/* Raster tuning (no counterpart in the reference; used by the autotuner):
+ * phase = triangles rasterised between hierarchical-z refreshes (0: 16),
+ * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
+gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
 /* Record per-stage CUDA-event times into gbr_stats (off by default). */
 gbr_status gbr_set_timing(gbr_renderer *r, int enabled);
 
@@ -150,6 +176,65 @@ gbr_status gbr_get_bins(gbr_renderer *r, uint32_t *offsets, uint32_t *ids, uint6
 /* GetTotalNumVisibleTriangles / GetTotalNumTriangles and per-stage timers
  * (CUDARenderer.h:63-73); synchronises with `stream`. */
 gbr_status gbr_get_stats(gbr_renderer *r, gbr_stats *out, void *stream);
+
+/* Batched frames (no counterpart in the reference, whose Render() draws one
+ * scene with one launch chain per mesh and per 256-triangle chunk,
+ * CUDARenderer.cu:249-339).  A batch renders many renderers' scenes -- each
+ * with its own resolution, meshes, textures, camera and render state -- as
+ * one frame: six launches in total (reset, setup + count, per-scene scan,
+ * fill, one persistent raster over the (scene, bin) work queue of every
+ * scene, shade), replayed from a CUDA graph.  All scenes of a batch use the
+ * batch's square bin size and queue chunk; each scene's output lands in its
+ * renderer's frame buffers.  A renderer in a batch cannot be destroyed
+ * until the batch is; its scene may change between batch frames. */
+typedef struct gbr_batch gbr_batch;
+typedef struct {
+    uint32_t bin_size;     /* bins of bin_size x bin_size pixels, 1..64 */
+    uint32_t queue_chunk;  /* bin-list entries per raster work item, >= 1 */
+    uint32_t raster_ctas;  /* raster variant: CTAs per SM, 2..6 (0: 6) */
+    uint32_t raster_phase; /* triangles between hierarchical-z refreshes (0: 16) */
+} gbr_batch_config;
+typedef struct {
+    uint32_t num_scenes;
+    uint32_t graph_captures;  /* CUDA graphs captured so far (layout or storage changes) */
+    uint32_t overflow_reruns; /* batch frames re-rendered after outgrowing the bin storage */
+    uint32_t pad;
+    uint64_t num_triangles, num_visible, num_pairs, num_work_items;
+    float ms_frame;           /* device time of the last batch frame (timing on) */
+    float pad2;
+} gbr_batch_stats;
+
+gbr_status gbr_batch_create(gbr_batch **out);
+gbr_status gbr_batch_destroy(gbr_batch *b);
+/* Adds renderer r with the camera and render state it is drawn with;
+ * *index numbers it in the batch. */
+gbr_status gbr_batch_add(gbr_batch *b, gbr_renderer *r, const gbr_camera *cam, uint32_t cull, uint32_t sample,
+                         uint32_t vis, uint32_t *index);
+gbr_status gbr_batch_set_view(gbr_batch *b, uint32_t index, const gbr_camera *cam, uint32_t cull, uint32_t sample,
+                              uint32_t vis);
+gbr_status gbr_batch_set_config(gbr_batch *b, const gbr_batch_config *cfg);
+gbr_status gbr_batch_get_config(const gbr_batch *b, gbr_batch_config *cfg);
+/* Times `frames` batch frames (after one warm-up frame) for every
+ * combination of the candidate bin sizes, queue chunks and raster variants
+ * (a NULL list keeps the current value) and keeps the fastest; *best gets
+ * it.  Synchronises `stream`. */
+gbr_status gbr_batch_autotune(gbr_batch *b, const uint32_t *bin_sizes, uint32_t num_bin_sizes, const uint32_t *chunks,
+                              uint32_t num_chunks, const uint32_t *raster_ctas, uint32_t num_raster_ctas,
+                              uint32_t frames, void *stream, gbr_batch_config *best);
+gbr_status gbr_batch_set_timing(gbr_batch *b, int enabled);
+/* One batch frame on `stream`, without host synchronisation. */
+gbr_status gbr_batch_render(gbr_batch *b, void *stream);
+/* Synchronise `stream` (re-rendering the batch if it outgrew its bin
+ * storage) and report the last batch frame. */
+gbr_status gbr_batch_get_stats(gbr_batch *b, gbr_batch_stats *out, void *stream);
+/* Bin grid of scene `index` under the current configuration. */
+gbr_status gbr_batch_scene_bins(const gbr_batch *b, uint32_t index, uint32_t *num_bins_x, uint32_t *num_bins_y);
+/* As gbr_readback / gbr_readback_ids / gbr_get_bins for scene `index` of the
+ * last batch frame (any output pointer may be NULL). */
+gbr_status gbr_batch_readback(gbr_batch *b, uint32_t index, uint32_t *colour, float *depth, uint32_t *ids,
+                              void *stream);
+gbr_status gbr_batch_get_bins(gbr_batch *b, uint32_t index, uint32_t *offsets, uint32_t *ids, uint64_t capacity,
+                              uint64_t *num_pairs, void *stream);
 
 /* No counterpart in the reference.  Renders one frame of one mesh (vertex
  * colours; no textures) from device-resident vertices into caller-owned

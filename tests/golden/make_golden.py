@@ -32,7 +32,6 @@ import numpy as np  # noqa: E402
 import scenes  # noqa: E402
 from oracle.ref import build_ref, ref_io  # noqa: E402
 
-BAND = (500, 532)  # rows kept for full-size frames
 
 
 def two_sphere_scene():
@@ -55,8 +54,9 @@ CASES = {
     "soup5k_256x192": lambda: scenes.soup_scene(5000, 256, 192, seed=101),
     "soup5k_256x192_backface": lambda: scenes.soup_scene(5000, 256, 192, seed=102, cull=scenes.CULL_BACKFACE),
     "soup1m_1080p": lambda: scenes.soup_scene(1_000_000, 1920, 1080, seed=0),
+    "icosphere7_4k": lambda: scenes.icosphere_scene(),
 }
-FULL_SIZE = {"soup1m_1080p"}
+FULL_SIZE = {"soup1m_1080p": (500, 532), "icosphere7_4k": (1064, 1096)}
 
 
 def scene_hash(path):
@@ -86,9 +86,10 @@ def run_case(name, out_dir, harness):
             "bins_sha256": bins_hash(offsets, ids), "width": scene.width, "height": scene.height}
     arrays = {}
     if name in FULL_SIZE:
-        meta["rows"] = list(BAND)
-        arrays["colour"] = res["colour"][BAND[0]:BAND[1]]
-        arrays["z"] = res["z"][BAND[0]:BAND[1]]
+        band = FULL_SIZE[name]
+        meta["rows"] = list(band)
+        arrays["colour"] = res["colour"][band[0]:band[1]]
+        arrays["z"] = res["z"][band[0]:band[1]]
     else:
         meta["rows"] = [0, scene.height]
         arrays["colour"] = res["colour"]

@@ -1,0 +1,110 @@
+"""The bin-capacity model.
+
+CPU: the float64 oracle's gradient (oracle/mlp_oracle.py) against central
+finite differences, so it can judge the GPU kernels.
+GPU: the training kernels' forward and loss + gradient (BF16 parameters,
+FP32 accumulation) against the oracle; predicted-capacity binning gives bin
+lists and images identical to exact binning, both when the capacities hold
+and when a bin overflows and the frame is re-binned on the device.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import scenes
+from oracle import mlp_oracle
+
+
+def random_problem(n=96, seed=0, scale=0.3):
+    rng = np.random.default_rng(seed)
+    w = mlp_oracle.f32_to_bf16(rng.normal(0, scale, mlp_oracle.NUM_PARAMS))
+    X = rng.normal(0.5, 1.0, (n, mlp_oracle.F)).astype(np.float32)
+    y = rng.integers(0, 400, n).astype(np.float32)
+    return w, X, y
+
+
+def test_oracle_gradient_matches_finite_differences():
+    w16, X, y = random_problem(16, seed=1)
+    w = mlp_oracle.bf16_to_f64(w16)
+    _, g = mlp_oracle.loss_grad(w16, X, y)
+
+    def loss_at(wv):
+        W1, b1, W2, b2, W3, b3 = mlp_oracle.unpack(wv)
+        h1 = np.maximum(X @ W1 + b1, 0)
+        h2 = np.maximum(h1 @ W2 + b2, 0)
+        lam = mlp_oracle.softplus(h2 @ W3 + b3)
+        return float(((np.log1p(lam) - np.log1p(y)) ** 2).sum())
+
+    rng = np.random.default_rng(2)
+    for i in rng.choice(mlp_oracle.NUM_PARAMS, 60, replace=False).tolist() + [mlp_oracle.OFF_B3]:
+        e = np.zeros_like(w)
+        e[i] = 1e-6
+        fd = (loss_at(w + e) - loss_at(w - e)) / 2e-6
+        assert abs(fd - g[i]) <= 1e-4 * max(1.0, abs(fd)), (i, fd, g[i])
+
+
+@pytest.mark.gpu
+def test_gpu_loss_gradient_and_forward_match_oracle(gbr_lib, cuda_device):
+    import torch
+    L = gbr_lib.lib()
+    assert L.gbr_mlp_num_params() == mlp_oracle.NUM_PARAMS
+    w16, X, y = random_problem(200, seed=3)
+    dw = torch.from_numpy(w16.view(np.int16)).to(cuda_device)
+    dX = torch.from_numpy(X).to(cuda_device)
+    dy = torch.from_numpy(y).to(cuda_device)
+    grad = torch.zeros(mlp_oracle.NUM_PARAMS, device=cuda_device)
+    loss = torch.zeros(1, device=cuda_device)
+    out = torch.empty(len(y), device=cuda_device)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    gbr_lib.check(L.gbr_mlp_loss_grad(p(dw), p(dX), p(dy), len(y), p(grad), p(loss), None))
+    gbr_lib.check(L.gbr_mlp_predict(p(dw), p(dX), len(y), p(out), None))
+    torch.cuda.synchronize()
+    ref_loss, ref_grad = mlp_oracle.loss_grad(w16, X, y)
+    g = grad.cpu().numpy().astype(np.float64)
+    assert abs(float(loss.item()) - ref_loss) <= 1e-4 * abs(ref_loss)
+    scale = np.abs(ref_grad).max()
+    assert np.abs(g - ref_grad).max() <= 2e-4 * scale, np.abs(g - ref_grad).max() / scale
+    lam = out.cpu().numpy().astype(np.float64)
+    ref_lam = mlp_oracle.predict(w16, X)
+    assert np.allclose(lam, ref_lam, rtol=1e-4, atol=1e-5)
+
+
+def _frame(gbr, scene, predictor=None):
+    r = gbr.Renderer(scene.width, scene.height)
+    r.load_scene(scene)
+    if predictor is not None:
+        w, a, b, g = predictor
+        gbr.check(r._lib.gbr_set_predictor(r.h, w.ctypes.data_as(C.c_void_p), len(w), C.c_float(a), C.c_float(b),
+                                           C.c_float(g)))
+        r.set_binning(gbr.BINNING_PREDICTED)
+        # a first frame sizes the bin storage for the predicted capacities
+        r.render_scene(scene)
+        r.stats()
+    r.render_scene(scene)
+    colour, depth = r.readback()
+    ids = r.readback_ids()
+    offsets, bins = r.get_bins()
+    st = r.stats()
+    r.close()
+    return colour, depth, ids, offsets, bins, st
+
+
+def _constant_model(count: float) -> np.ndarray:
+    """A model that predicts `count` for every bin (all weights zero, output
+    bias softplus^-1(count))."""
+    w = np.zeros(mlp_oracle.NUM_PARAMS, np.float32)
+    w[mlp_oracle.OFF_B3] = count + np.log(-np.expm1(-count))
+    return mlp_oracle.f32_to_bf16(w)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("count,expect_overflow", [(40000.0, False), (2.0, True)])
+def test_predicted_binning_is_identical_to_exact(gbr_lib, cuda_device, count, expect_overflow):
+    s = scenes.soup_scene(60000, 640, 480, seed=41)
+    exact = _frame(gbr_lib, s)
+    pred = _frame(gbr_lib, s, (_constant_model(count), 0.0, 0.0, 0.0))
+    assert pred[5]["predicted_overflow"] == (1 if expect_overflow else 0)
+    for a, b in zip(exact[:5], pred[:5]):
+        assert np.array_equal(a, b)
+    assert pred[5]["num_pairs"] == exact[5]["num_pairs"] and pred[5]["num_visible"] == exact[5]["num_visible"]
