@@ -115,6 +115,12 @@ void gbr::frame_basics(const gbr_renderer* r, const gbr_camera* cam, uint32_t cu
     F.num_tris = (uint32_t)scene_triangles(r);
     for (int k = 0; k < 3; ++k) { F.cam_pos[k] = cam->pos[k]; F.cam_fwd[k] = cam->fwd[k]; }
     F.colour = r->d_colour; F.depth = r->d_depth; F.ids = r->d_ids; F.gvis = r->d_gvis;
+    F.lights = r->d_lights;
+    F.num_lights = r->num_lights;
+    bool textured = false;
+    for (const MeshHost& m : r->meshes) textured |= m.tex_ids[0] >= 0 && (size_t)m.tex_ids[0] < r->textures.size() &&
+                                                   r->textures[m.tex_ids[0]].d_px;
+    F.flat_shade = vis == GBR_VIS_PBR && !textured ? 1u : 0u;
 }
 
 namespace {
@@ -127,7 +133,8 @@ uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_
 
 void free_bins(gbr_renderer* r) {
     cudaFree(r->d_counts); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
-    cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list);
+    cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_partial);
+    r->d_partial = nullptr;
     cudaFree(r->d_feat); cudaFree(r->d_features_out);
     r->d_feat = nullptr;
     r->d_features_out = nullptr;
@@ -244,6 +251,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.items = r->d_items; F.items_cap = r->items_cap;
     F.list = r->d_list; F.list_cap = r->list_cap;
     F.ctl = r->d_ctl;
+    F.scan_partial = r->d_partial;
     const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
     F.feat = r->d_feat;
     F.mlp_w = r->d_mlp_w;
@@ -259,12 +267,12 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         // exact kernels behind it only run if a bin overflowed
         GBR_CUDA(launch_prepass(F, s));
         GBR_CUDA(launch_capacity(F, true, s));
-        GBR_CUDA(launch_scan(F, true, s));
+        GBR_CUDA(launch_scan(scan_of(F, kScanCapacity), s));
         GBR_CUDA(launch_setup(F, true, s));
         if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
-        GBR_CUDA(launch_items(F, s));
+        GBR_CUDA(launch_scan(scan_of(F, kScanPredictedItems), s));
         GBR_CUDA(launch_setup(F, false, s));
-        GBR_CUDA(launch_scan(F, false, s));
+        GBR_CUDA(launch_scan(scan_of(F, kScanExactAfterPredicted), s));
         GBR_CUDA(launch_fill(F, s));
     } else {
         if (r->collect) {
@@ -274,7 +282,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         }
         GBR_CUDA(launch_setup(F, false, s));
         if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
-        GBR_CUDA(launch_scan(F, false, s));
+        GBR_CUDA(launch_scan(scan_of(F, kScanExact), s));
         GBR_CUDA(launch_fill(F, s));
     }
     r->last_predicted = predicted;
@@ -306,10 +314,12 @@ gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
         GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     }
     if (r->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "bin storage overflow persists");
-    // predicted capacities that did not fit the list: grow it for the next frames
-    if (r->last_predicted && r->h_ctl->pred_capacity > r->list_cap) {
-        gbr_status st = ensure_list(r, r->h_ctl->pred_capacity);
-        if (st != GBR_OK) return st;
+    // predicted capacities that did not fit the list: grow it for the next
+    // frames, within reason (the frame itself was re-binned exactly)
+    const uint64_t want = r->h_ctl->pred_capacity;
+    if (r->last_predicted && want > r->list_cap && want <= 0x7FFFFFFFull &&
+        want <= 16u * r->h_ctl->num_pairs + (1u << 22)) {
+        if (ensure_list(r, want) != GBR_OK) ensure_list(r, r->h_ctl->num_pairs);
     }
     return GBR_OK;
 }
@@ -345,6 +355,7 @@ gbr_status gbr_create(uint32_t width, uint32_t height, gbr_renderer** out) {
     if (e == cudaSuccess) e = cudaMalloc(&r->d_ctl, sizeof(Ctl));
     if (e == cudaSuccess) e = cudaMemset(r->d_ctl, 0, sizeof(Ctl));
     if (e == cudaSuccess) e = cudaMallocHost(&r->h_ctl, sizeof(Ctl));
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_lights, kMaxLights * sizeof(LightDev));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->meshes_evt, cudaEventDisableTiming);
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&r->ev[i]);
     if (e != cudaSuccess) {
@@ -364,6 +375,7 @@ gbr_status gbr_destroy(gbr_renderer* r) {
     free_bins(r);
     cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis);
     cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_meshes); cudaFree(r->d_ctl); cudaFree(r->d_mlp_w);
+    cudaFree(r->d_lights);
     cudaFreeHost(r->h_meshes); cudaFreeHost(r->h_ctl);
     if (r->meshes_evt) cudaEventDestroy(r->meshes_evt);
     for (int i = 0; i < 5; ++i)
@@ -393,6 +405,7 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     GBR_CUDA(cudaMalloc(&r->d_capacity, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_capacity, 0, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_bin_done, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_partial, 2u * scan_blocks(nb) * sizeof(unsigned long long)));
     GBR_CUDA(cudaMemset(r->d_bin_done, 0, nb * sizeof(uint32_t)));
     // pre-pass accumulators: slot 4 (depth min) starts at all ones, the rest at 0
     GBR_CUDA(cudaMalloc(&r->d_feat, (size_t)kFeatSlots * nb * sizeof(uint32_t)));
@@ -538,6 +551,19 @@ gbr_status gbr_texture_remove(gbr_renderer* r, int32_t tex_id) {
     return GBR_OK;
 }
 
+gbr_status gbr_set_lights(gbr_renderer* r, const gbr_light* lights, uint32_t n) {
+    if (!r || (n && !lights) || n > kMaxLights) return fail(GBR_ERR_INVALID_ARG, "bad renderer or lights (n %u, max %u)", n, kMaxLights);
+    static_assert(sizeof(gbr_light) == sizeof(LightDev), "gbr_light mirrors the device record");
+    for (uint32_t k = 0; k < n; ++k)
+        if (lights[k].type > GBR_LIGHT_POINT) return fail(GBR_ERR_INVALID_ARG, "light %u: unknown type %u", k, lights[k].type);
+    if (n) {
+        cudaDeviceSynchronize();   // frames in flight read the previous lights
+        GBR_CUDA(cudaMemcpy(r->d_lights, lights, n * sizeof(LightDev), cudaMemcpyHostToDevice));
+    }
+    r->num_lights = n;
+    return GBR_OK;
+}
+
 gbr_status gbr_set_binning(gbr_renderer* r, uint32_t method) {
     if (!r || method > GBR_BINNING_PREDICTED) return fail(GBR_ERR_INVALID_ARG, "bad renderer or binning method");
     r->binning = method;
@@ -567,7 +593,7 @@ gbr_status gbr_render(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, uin
                       void* stream) {
     if (!r || !cam) return fail(GBR_ERR_INVALID_ARG, "null renderer or camera");
     if (!r->bins_ready) return fail(GBR_ERR_INVALID_ARG, "gbr_setup_bins was not called");
-    if (cull > GBR_CULL_NONE || sample > GBR_SAMPLE_LINEAR || vis > GBR_VIS_NORMAL)
+    if (cull > GBR_CULL_NONE || sample > GBR_SAMPLE_BILINEAR || vis > GBR_VIS_NORMAL)
         return fail(GBR_ERR_INVALID_ARG, "bad cull/sample/vis (%u/%u/%u)", cull, sample, vis);
     return render_frame(r, cam, cull, sample, vis, (cudaStream_t)stream);
 }

@@ -42,7 +42,7 @@ struct Member {
 struct SceneLayout {
     uint32_t W = 0, H = 0, nbx = 0, nby = 0, num_meshes = 0;
     uint64_t tris = 0;
-    uint32_t bin_base = 0, offsets_base = 0, mesh_base = 0;
+    uint32_t bin_base = 0, mesh_base = 0;
     uint64_t tri_base = 0;
 };
 
@@ -68,6 +68,7 @@ struct gbr_batch {
     uint32_t* d_counts = nullptr;
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
+    unsigned long long* d_partial = nullptr;   // bin scan scratch
     TriSetup* d_setup = nullptr;
     uint2* d_rects = nullptr;
     uint32_t* d_list = nullptr;
@@ -107,8 +108,9 @@ void drop_graph(gbr_batch* b) {
 
 void free_layout_storage(gbr_batch* b) {
     cudaFree(b->d_tables); cudaFree(b->d_counts); cudaFree(b->d_offsets); cudaFree(b->d_cursors);
-    cudaFree(b->d_setup); cudaFree(b->d_rects);
+    cudaFree(b->d_setup); cudaFree(b->d_rects); cudaFree(b->d_partial);
     b->d_tables = b->d_counts = b->d_offsets = b->d_cursors = nullptr;
+    b->d_partial = nullptr;
     b->d_setup = nullptr;
     b->d_rects = nullptr;
 }
@@ -154,7 +156,7 @@ gbr_status ensure_layout(gbr_batch* b) {
     drop_graph(b);
     free_layout_storage(b);
     b->layout.assign(n, SceneLayout());
-    uint64_t bins = 0, offsets = 0, tris = 0, tri_blocks = 0, px_blocks = 0;
+    uint64_t bins = 0, tris = 0, tri_blocks = 0, px_blocks = 0;
     uint32_t meshes = 0;
     std::vector<uint32_t> tables(3u * (n + 1u));
     for (uint32_t i = 0; i < n; ++i) {
@@ -168,14 +170,12 @@ gbr_status ensure_layout(gbr_batch* b) {
         L.tris = scene_triangles(r);
         if (L.tris >= 0x7FFFFFFFull) return fail(GBR_ERR_INVALID_ARG, "scene %u has too many triangles", i);
         L.bin_base = (uint32_t)bins;
-        L.offsets_base = (uint32_t)offsets;
         L.mesh_base = meshes;
         L.tri_base = tris;
         tables[i] = (uint32_t)tri_blocks;
         tables[(n + 1u) + i] = (uint32_t)px_blocks;
         tables[2u * (n + 1u) + i] = (uint32_t)bins;
         bins += (uint64_t)L.nbx * L.nby;
-        offsets += (uint64_t)L.nbx * L.nby + 1u;
         tris += L.tris;
         meshes += L.num_meshes;
         tri_blocks += ceil_div(L.tris, 256u);
@@ -197,7 +197,10 @@ gbr_status ensure_layout(gbr_batch* b) {
     GBR_CUDA(cudaMemcpy(b->d_tables, tables.data(), tables.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     GBR_CUDA(cudaMalloc(&b->d_counts, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(b->d_counts, 0, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
-    GBR_CUDA(cudaMalloc(&b->d_offsets, std::max<uint64_t>(offsets, 1u) * sizeof(uint32_t)));
+    // one scan over the bins of every scene: scene s's offsets are entries
+    // [bin_base[s], bin_base[s+1]] of the batch-wide array
+    GBR_CUDA(cudaMalloc(&b->d_offsets, (bins + 1u) * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&b->d_partial, 2u * scan_blocks((uint32_t)bins) * sizeof(unsigned long long)));
     GBR_CUDA(cudaMalloc(&b->d_cursors, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&b->d_setup, std::max<uint64_t>(tris, 1u) * sizeof(TriSetup)));
     GBR_CUDA(cudaMalloc(&b->d_rects, std::max<uint64_t>(tris, 1u) * sizeof(uint2)));
@@ -250,7 +253,7 @@ void build_table(gbr_batch* b, std::vector<unsigned char>& out) {
         F.setup = b->d_setup + L.tri_base;
         F.rects = b->d_rects + L.tri_base;
         F.counts = b->d_counts + L.bin_base;
-        F.offsets = b->d_offsets + L.offsets_base;
+        F.offsets = b->d_offsets + L.bin_base;
         F.cursors = b->d_cursors + L.bin_base;
         F.list = b->d_list;
         F.list_cap = b->list_cap;
@@ -285,6 +288,18 @@ gbr_status capture_graph(gbr_batch* b) {
     L.raster_ctas = b->cfg.raster_ctas;
     L.bin_w = L.bin_h = b->cfg.bin_size;
     const BatchDev B = batch_dev(b);
+    memset(&L.scan, 0, sizeof L.scan);
+    L.scan.counts = b->d_counts;
+    L.scan.offsets = b->d_offsets;
+    L.scan.cursors = b->d_cursors;
+    L.scan.items = b->d_items;
+    L.scan.partial = b->d_partial;
+    L.scan.ctl = b->d_ctl;
+    L.scan.list_cap = b->list_cap;
+    L.scan.items_cap = b->items_cap;
+    L.scan.n = b->total_bins;
+    L.scan.chunk = b->cfg.queue_chunk;
+    L.scan.mode = kScanExact;
     GBR_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = launch_batch(B, L, b->cap_stream);
     cudaGraph_t g = nullptr;
@@ -339,7 +354,7 @@ gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
     GBR_CUDA(cudaStreamSynchronize(s));
     GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     for (int attempt = 0; b->h_ctl->overflow && attempt < 3; ++attempt) {
-        gbr_status st = ensure_list(b, b->h_ctl->num_pairs, b->h_ctl->num_items);
+        gbr_status st = ensure_list(b, b->h_ctl->num_pairs, b->h_ctl->items_alloc);
         if (st != GBR_OK) return st;
         ++b->overflow_reruns;
         st = render_batch(b, s);
@@ -352,7 +367,7 @@ gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
 }
 
 gbr_status check_state(uint32_t cull, uint32_t sample, uint32_t vis) {
-    if (cull > GBR_CULL_NONE || sample > GBR_SAMPLE_LINEAR || vis > GBR_VIS_NORMAL)
+    if (cull > GBR_CULL_NONE || sample > GBR_SAMPLE_BILINEAR || vis > GBR_VIS_NORMAL)
         return fail(GBR_ERR_INVALID_ARG, "bad cull/sample/vis (%u/%u/%u)", cull, sample, vis);
     return GBR_OK;
 }
@@ -536,7 +551,7 @@ gbr_status gbr_batch_get_stats(gbr_batch* b, gbr_batch_stats* out, void* stream)
     out->overflow_reruns = b->overflow_reruns;
     out->graph_captures = b->graph_captures;
     out->num_pairs = b->h_ctl->num_pairs;
-    out->num_work_items = b->h_ctl->num_items;
+    out->num_work_items = b->h_ctl->items_alloc;
     Ctl c;
     for (const Member& m : b->members) {
         GBR_CUDA(cudaMemcpy(&c, m.r->d_ctl, sizeof c, cudaMemcpyDeviceToHost));
@@ -579,7 +594,7 @@ gbr_status gbr_batch_get_bins(gbr_batch* b, uint32_t index, uint32_t* offsets, u
     const SceneLayout& L = b->layout[index];
     const uint32_t nb = L.nbx * L.nby;
     std::vector<uint32_t> off(nb + 1u);
-    GBR_CUDA(cudaMemcpy(off.data(), b->d_offsets + L.offsets_base, (nb + 1u) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    GBR_CUDA(cudaMemcpy(off.data(), b->d_offsets + L.bin_base, (nb + 1u) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     const uint64_t total = (uint64_t)off[nb] - off[0];
     if (num_pairs) *num_pairs = total;
     if (offsets)

@@ -50,6 +50,16 @@ struct MeshDev {
     TexDev tex[4];
 };
 
+// A scene light (the build's shading extension; gbr_light in gbr.h).
+constexpr uint32_t kMaxLights = 8;
+struct LightDev {
+    uint32_t type;        // 0 directional (vec = travel direction), 1 point (vec = position)
+    float colour[3];
+    float intensity;
+    float vec[3];
+};
+static_assert(sizeof(LightDev) == 32, "light record is 32 bytes");
+
 // Raster setup record, 48 B: the triangle's float screen vertices (the
 // raster snaps them to 16.16 for coverage), NDC z per vertex, 1 / the float
 // area the reference divides its weights by, flags, mesh index.
@@ -75,8 +85,10 @@ struct Ctl {
     unsigned long long pred_capacity;
     uint32_t error;            // non-zero: a bounded wait gave up
     uint32_t num_sampled;      // visible triangles seen by the coarse pre-pass
-    uint32_t pad[4];
+    unsigned long long items_alloc;   // batch: work items requested by all scenes
+    uint32_t pad[2];
 };
+static_assert(sizeof(Ctl) == 64, "control block is 64 bytes");
 
 // Everything a kernel of the frame needs, passed by value.
 struct FrameDev {
@@ -110,11 +122,39 @@ struct FrameDev {
     uint32_t* feat;            // coarse pre-pass accumulators, kFeatSlots x num_bins (slot-major)
     const uint16_t* mlp_w;     // capacity model parameters, BF16
     float* features_out;       // optional: kFeatures features per bin (training data)
-    float cap_alpha, cap_beta, cap_gamma;  // capacity = ceil(l*(1+alpha) + beta*sqrt(l) + gamma)
-    uint32_t sample_stride;    // the pre-pass samples every sample_stride-th triangle
+    float cap_alpha, cap_beta, cap_gamma;  // capacity = ceil(l*(1+alpha) + beta*sqrt(l+1) + gamma)
+    uint32_t sample_stride;    // the pre-pass samples one triangle per group of sample_stride
     uint32_t exact_guard;      // exact-binning kernels run only after a predicted overflow
+    const LightDev* lights;    // scene lights (num_lights == 0: the reference shader's constant light)
+    uint32_t num_lights;
+    uint32_t flat_shade;      // PBR view and no mesh with a diffuse map: pixels shade from vertex colours
+    unsigned long long* scan_partial;   // bin scan scratch: 2 per block of 1024 bins
+    uint32_t pad_scan[2];
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
+
+// The bin scan (gbr_scan.cu) over n per-bin sizes.
+enum : uint32_t {
+    kScanExact = 0,                // exact counts -> offsets, cursors, work items
+    kScanCapacity = 1,             // predicted capacities -> offsets, cursors
+    kScanExactAfterPredicted = 2,  // as kScanExact, run only after a predicted overflow
+    kScanPredictedItems = 3        // filled sizes within the capacities -> work items
+};
+struct ScanDev {
+    uint32_t* counts;              // exact counts, zeroed for the next frame
+    const uint32_t* capacity;      // predicted capacities
+    uint32_t* offsets;             // n + 1
+    uint32_t* cursors;
+    uint4* items;
+    unsigned long long* partial;   // 2 per block of 1024 bins
+    Ctl* ctl;
+    uint32_t* feat;                // kScanPredictedItems: pre-pass accumulators to reset (or null)
+    unsigned long long list_cap;
+    uint32_t items_cap;
+    uint32_t n;
+    uint32_t chunk;
+    uint32_t mode;
+};
 
 // Many scenes rendered as one batch frame.  Each scene keeps its own frame
 // descriptor (its resolution, bins, meshes, frame buffers, statistics
@@ -335,6 +375,96 @@ __device__ __forceinline__ bool weights_float(const TriSetup& t, float px, float
     w[1] = __fdiv_rn(w[1], area);
     w[2] = __fdiv_rn(w[2], area);
     return true;
+}
+
+// Walks the bins of the warp's packed rectangles; called by whole warps.
+// The warp's (triangle, bin) pairs are expanded load-balanced: pair k of the
+// warp belongs to the lane whose exclusive pair prefix is the largest one
+// <= k, so every iteration gives each lane its own pair whatever the spread
+// of rectangle sizes.
+// Mode 0: count (atomicAdd on counts), 1: fill (append entry), 2: predicted
+// fill (append within the bin's predicted capacity), 3: pre-pass count
+// (atomicAdd on the first feature slot).  GBR_BIN_AGGREGATE 0 (the
+// default) issues one atomic per pair; 1 groups the lanes of a warp that hit
+// the same bin with __match_any_sync and lets one lane do the group's
+// atomic.  On GB300 the grouped form measured ~10% slower on both the 1M
+// soup and the 4K icosphere (the MATCH instruction and the divergent leader
+// branch load the ADU pipe, 88% busy in the fill kernel, while same-bin
+// lanes are rare), so it is built only on request.
+#ifndef GBR_BIN_AGGREGATE
+#define GBR_BIN_AGGREGATE 0
+#endif
+template <int MODE>
+__device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t bx0 = rect.x & 0xFFFFu, bx1 = rect.x >> 16;
+    const uint32_t by0 = rect.y & 0xFFFFu, by1 = (rect.y >> 16) & 0x7FFFu;
+    uint32_t w = 0, n = 0;
+    if (valid && bx0 <= bx1 && by0 <= by1) {
+        w = bx1 - bx0 + 1u;
+        n = w * (by1 - by0 + 1u);
+    }
+    uint32_t incl = n;   // inclusive prefix of pair counts over the warp
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t excl = incl - n;
+    for (uint32_t base = 0; base < total; base += 32u) {   // warp-uniform
+        const uint32_t k = base + lane;
+        uint32_t o = 0;   // largest lane with excl <= k: the owner of pair k
+#pragma unroll
+        for (uint32_t step = 16; step >= 1; step >>= 1) {
+            const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, o + step);
+            if (e <= k) o += step;
+        }
+        const uint32_t j = k - __shfl_sync(0xFFFFFFFFu, excl, o);
+        const uint32_t ow = __shfl_sync(0xFFFFFFFFu, w, o);
+        const uint32_t obx = __shfl_sync(0xFFFFFFFFu, bx0, o);
+        const uint32_t oby = __shfl_sync(0xFFFFFFFFu, by0, o);
+        const uint32_t oentry = __shfl_sync(0xFFFFFFFFu, entry, o);
+        const bool act = k < total;
+        const uint32_t q = act ? j / ow : 0u;
+        const uint32_t bin = act ? (obx + (j - q * ow)) + (oby + q) * F.nbx : 0xFFFFFFFFu;
+#if GBR_BIN_AGGREGATE == 0
+        // one atomic per pair, no grouping
+        if (!act) continue;
+        if (MODE == 0) {
+            atomicAdd(&F.counts[bin], 1u);
+        } else if (MODE == 3) {
+            atomicAdd(&F.feat[bin], 1u);
+        } else {
+            const uint32_t pos = atomicAdd(&F.cursors[bin], 1u);
+            if (MODE == 1) F.list[pos] = oentry;
+            else if (pos < __ldg(&F.offsets[bin]) + __ldg(&F.capacity[bin])) F.list[pos] = oentry;
+            else atomicOr(&F.ctl->pred_overflow, 1u);
+        }
+        continue;
+#endif
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, bin);
+        if (!act) continue;
+        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+        const uint32_t cnt = (uint32_t)__popc(peers);
+        if (MODE == 0) {
+            if (lane == leader) atomicAdd(&F.counts[bin], cnt);
+        } else if (MODE == 3) {
+            if (lane == leader) atomicAdd(&F.feat[bin], cnt);
+        } else {
+            uint32_t pos0 = 0;
+            if (lane == leader) pos0 = atomicAdd(&F.cursors[bin], cnt);
+            pos0 = __shfl_sync(peers, pos0, (int)leader);
+            const uint32_t pos = pos0 + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            if (MODE == 1) {
+                F.list[pos] = oentry;
+            } else {
+                // cursors start at the bin's offset; the bin owns capacity[bin] slots
+                if (pos < __ldg(&F.offsets[bin]) + __ldg(&F.capacity[bin])) F.list[pos] = oentry;
+                else if (lane == leader) atomicOr(&F.ctl->pred_overflow, 1u);
+            }
+        }
+    }
 }
 
 }  // namespace gbr

@@ -78,6 +78,7 @@ struct gbr_renderer {
     uint32_t* d_cursors = nullptr;
     uint32_t* d_capacity = nullptr;
     uint32_t* d_bin_done = nullptr;
+    unsigned long long* d_partial = nullptr;   // bin scan scratch
     uint4* d_items = nullptr;
     uint32_t items_cap = 0;
     uint32_t* d_list = nullptr;
@@ -95,6 +96,9 @@ struct gbr_renderer {
 
     gbr::Ctl* d_ctl = nullptr;
     gbr::Ctl* h_ctl = nullptr;
+
+    gbr::LightDev* d_lights = nullptr;   // kMaxLights records
+    uint32_t num_lights = 0;
 
     bool have_frame = false;
     gbr_camera last_cam{};

@@ -35,44 +35,6 @@ __device__ __forceinline__ uint32_t find_mesh(const FrameDev& F, uint32_t prim) 
     return lo;
 }
 
-// Walks the bins of a packed rectangle; warp-aggregates equal bins.
-// Mode 0: count (atomicAdd on counts), mode 1: fill (append entry),
-// mode 2: predicted fill (append within a predicted capacity).
-template <int MODE>
-__device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid) {
-    int bx0 = (int)(rect.x & 0xFFFFu), bx1 = (int)(rect.x >> 16);
-    int by0 = (int)(rect.y & 0xFFFFu), by1 = (int)((rect.y >> 16) & 0x7FFFu);
-    bool more = valid && bx0 <= bx1 && by0 <= by1;
-    int bx = bx0, by = by0;
-    const uint32_t lane = lane_id();
-    for (;;) {
-        const unsigned act = __ballot_sync(0xFFFFFFFFu, more);
-        if (!act) break;
-        if (more) {
-            const uint32_t bin = (uint32_t)bx + (uint32_t)by * F.nbx;
-            const unsigned peers = __match_any_sync(act, bin);
-            const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-            const uint32_t n = (uint32_t)__popc(peers);
-            if (MODE == 0) {
-                if (lane == leader) atomicAdd(&F.counts[bin], n);
-            } else {
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(&F.cursors[bin], n);
-                base = __shfl_sync(peers, base, (int)leader);
-                const uint32_t pos = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-                if (MODE == 1) {
-                    F.list[pos] = entry;
-                } else {
-                    // cursors start at the bin's offset; the bin owns capacity[bin] slots
-                    if (pos < __ldg(&F.offsets[bin]) + __ldg(&F.capacity[bin])) F.list[pos] = entry;
-                    else if (lane == leader) atomicOr(&F.ctl->pred_overflow, 1u);
-                }
-            }
-            if (++bx > bx1) { bx = bx0; if (++by > by1) more = false; }
-        }
-    }
-}
-
 // Vertex stage (positions), triangle assembly, cull, frustum reject, raster
 // setup record and bin rectangle of triangle `prim`, then the count pass
 // (MODE 0) or the predicted-capacity fill (MODE 1).  Called by whole warps.
@@ -161,70 +123,6 @@ __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
     // predicted pass stops once an overflow is known
     if (MODE == 0 ? (F.exact_guard && !F.ctl->pred_overflow) : (F.ctl->pred_overflow != 0u)) return;
     setup_tri<MODE>(F, blockIdx.x * blockDim.x + threadIdx.x);
-}
-
-// Single CTA.  counts -> offsets (exclusive, num_bins + 1), cursors, work
-// items; zeroes counts for the next frame.  predicted: capacities replace
-// counts for the offsets, and items are built later by pred_items.
-template <bool PREDICTED>
-__global__ void __launch_bounds__(1024) scan_kernel(FrameDev F) {
-    __shared__ uint32_t s_a[1024];
-    __shared__ uint32_t s_b[1024];
-    if (!PREDICTED && F.exact_guard && !F.ctl->pred_overflow) return;
-    const uint32_t nb = F.num_bins;
-    const uint32_t per = (nb + blockDim.x - 1u) / blockDim.x;
-    const uint32_t b0 = threadIdx.x * per;
-    const uint32_t b1 = min(b0 + per, nb);
-    const uint32_t chunk = F.chunk;
-    uint32_t sum = 0, items = 0;
-    for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t c = PREDICTED ? F.capacity[b] : F.counts[b];
-        sum += c;
-        items += c == 0u ? 1u : (c + chunk - 1u) / chunk;
-    }
-    s_a[threadIdx.x] = sum;
-    s_b[threadIdx.x] = items;
-    __syncthreads();
-    // Hillis-Steele inclusive scan over 1024 partials (counts < 2^32 total)
-    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
-        const uint32_t a = threadIdx.x >= off ? s_a[threadIdx.x - off] : 0u;
-        const uint32_t c = threadIdx.x >= off ? s_b[threadIdx.x - off] : 0u;
-        __syncthreads();
-        s_a[threadIdx.x] += a;
-        s_b[threadIdx.x] += c;
-        __syncthreads();
-    }
-    uint32_t run = s_a[threadIdx.x] - sum;
-    uint32_t item = s_b[threadIdx.x] - items;
-    const uint32_t total = s_a[blockDim.x - 1u];
-    const uint32_t total_items = s_b[blockDim.x - 1u];
-    const bool fits = (unsigned long long)total <= F.list_cap && total_items <= F.items_cap;
-    for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t c = PREDICTED ? F.capacity[b] : F.counts[b];
-        F.offsets[b] = run;
-        F.cursors[b] = run;
-        if (!PREDICTED) {
-            F.counts[b] = 0u;
-            const uint32_t n = c == 0u ? 1u : (c + chunk - 1u) / chunk;
-            if (fits)
-                for (uint32_t k = 0; k < n; ++k)
-                    F.items[item + k] = make_uint4(b, run + k * chunk, min(chunk, c - min(c, k * chunk)), n);
-            item += n;
-        }
-        run += c;
-    }
-    if (threadIdx.x == 0) {
-        F.offsets[nb] = total;
-        if (PREDICTED) {
-            F.ctl->pred_capacity = total;
-            if ((unsigned long long)total > F.list_cap) F.ctl->pred_overflow = 1u;
-        } else {
-            F.ctl->num_pairs = total;
-            F.ctl->num_items = fits ? total_items : 0u;
-            F.ctl->item_next = 0u;
-            if (!fits) F.ctl->overflow = 1u;
-        }
-    }
 }
 
 // Second pass of exact binning for triangle `prim`.  Called by whole warps.
@@ -358,6 +256,7 @@ __device__ __forceinline__ void raster_float(const TriSetup& t, uint32_t prim, u
     }
 }
 
+template <bool FLAT>
 __device__ __forceinline__ void resolve_pixel(const FrameDev& F, int x, int y, unsigned long long v) {
     const size_t gi = (size_t)y * F.width + (size_t)x;
     if (v == kEmptyVis) {
@@ -378,7 +277,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& F, int x, int y, u
     else weights_fixed(t, x, y, w);
     const float z = interp_z(w[0], w[1], w[2], t.z0, t.z1, t.z2);
     const MeshDev& m = F.meshes[t.mesh];
-    F.colour[gi] = shade_fragment(F, m, prim, w, z);
+    F.colour[gi] = shade_fragment<FLAT>(F, m, prim, w, z);
     F.depth[gi] = z;
     F.ids[gi] = prim;
 }
@@ -535,17 +434,19 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
 // Shades pixel i of the frame: the winner the raster left in the merge
 // buffer (or the clear colour), and leaves the buffer empty for the next
 // frame.
+template <bool FLAT>
 __device__ __forceinline__ void shade_px(const FrameDev& F, uint32_t i) {
     const unsigned long long v = F.gvis[i];
     if (v != kEmptyVis) F.gvis[i] = kEmptyVis;
-    resolve_pixel(F, (int)(i % F.width), (int)(i / F.width), v);
+    resolve_pixel<FLAT>(F, (int)(i % F.width), (int)(i / F.width), v);
 }
 
 // One thread per pixel.
+template <bool FLAT>
 __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.width * F.height || F.ctl->overflow) return;
-    shade_px(F, i);
+    shade_px<FLAT>(F, i);
 }
 
 // Pixels no bin covers (num_bins * bin_dim smaller than the screen).
@@ -601,74 +502,6 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
     setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x);
 }
 
-// One CTA per scene: the scene's bin counts -> list offsets, fill cursors
-// and work items.  The scene's list range and item range are allocated
-// from the batch's counters; a range past the storage raises the batch's
-// overflow flag (the later stages then do nothing and the host re-renders
-// the batch with larger storage).
-__global__ void __launch_bounds__(1024) batch_scan_kernel(BatchDev B) {
-    __shared__ uint32_t s_a[1024];
-    __shared__ uint32_t s_b[1024];
-    __shared__ __align__(16) FrameDev sF;
-    __shared__ uint32_t s_run, s_item, s_fits;
-    const uint32_t sc = blockIdx.x;
-    load_scene(B, sc, sF);
-    const FrameDev& F = sF;
-    const uint32_t nb = F.num_bins;
-    const uint32_t per = (nb + blockDim.x - 1u) / blockDim.x;
-    const uint32_t b0 = threadIdx.x * per;
-    const uint32_t b1 = min(b0 + per, nb);
-    const uint32_t chunk = F.chunk;
-    uint32_t sum = 0, items = 0;
-    for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t c = F.counts[b];
-        sum += c;
-        items += c == 0u ? 1u : (c + chunk - 1u) / chunk;
-    }
-    s_a[threadIdx.x] = sum;
-    s_b[threadIdx.x] = items;
-    __syncthreads();
-    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
-        const uint32_t a = threadIdx.x >= off ? s_a[threadIdx.x - off] : 0u;
-        const uint32_t c = threadIdx.x >= off ? s_b[threadIdx.x - off] : 0u;
-        __syncthreads();
-        s_a[threadIdx.x] += a;
-        s_b[threadIdx.x] += c;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const uint32_t total = s_a[blockDim.x - 1u];
-        const uint32_t total_items = s_b[blockDim.x - 1u];
-        const unsigned long long run0 = atomicAdd(&B.ctl->num_pairs, (unsigned long long)total);
-        const uint32_t item0 = atomicAdd(&B.ctl->num_items, total_items);
-        const bool fits = run0 + total <= B.list_cap && (unsigned long long)item0 + total_items <= B.items_cap;
-        if (!fits) atomicOr(&B.ctl->overflow, 1u);
-        s_run = fits ? (uint32_t)run0 : 0u;
-        s_item = item0;
-        s_fits = fits ? 1u : 0u;
-        F.ctl->num_pairs = total;
-        F.ctl->num_items = total_items;
-        F.offsets[nb] = s_run + total;
-    }
-    __syncthreads();
-    const bool fits = s_fits != 0u;
-    const uint32_t gbin = __ldg(B.bin_base + sc);
-    uint32_t run = s_run + s_a[threadIdx.x] - sum;
-    uint32_t item = s_item + s_b[threadIdx.x] - items;
-    for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t c = F.counts[b];
-        F.offsets[b] = run;
-        F.cursors[b] = run;
-        F.counts[b] = 0u;
-        const uint32_t n = c == 0u ? 1u : (c + chunk - 1u) / chunk;
-        if (fits)
-            for (uint32_t k = 0; k < n; ++k)
-                B.items[item + k] = make_uint4(gbin + b, run + k * chunk, min(chunk, c - min(c, k * chunk)), n);
-        item += n;
-        run += c;
-    }
-}
-
 __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
     if (B.ctl->overflow) return;
     __shared__ __align__(16) FrameDev sF;
@@ -683,7 +516,9 @@ __global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {
     __shared__ uint32_t s_sc;
     const uint32_t sc = block_scene(B, B.px_blocks, sF, s_sc);
     const uint32_t i = (blockIdx.x - __ldg(B.px_blocks + sc)) * 256u + threadIdx.x;
-    if (i < sF.width * sF.height) shade_px(sF, i);
+    if (i >= sF.width * sF.height) return;
+    if (sF.flat_shade) shade_px<true>(sF, i);
+    else shade_px<false>(sF, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -698,12 +533,6 @@ cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s) {
     if (blocks == 0) return cudaSuccess;
     if (predicted) setup_kernel<1><<<blocks, 256, 0, s>>>(F);
     else setup_kernel<0><<<blocks, 256, 0, s>>>(F);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_scan(const FrameDev& F, bool predicted, cudaStream_t s) {
-    if (predicted) scan_kernel<true><<<1, 1024, 0, s>>>(F);
-    else scan_kernel<false><<<1, 1024, 0, s>>>(F);
     return cudaGetLastError();
 }
 
@@ -733,7 +562,8 @@ cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
     cudaError_t e = launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
     if (e != cudaSuccess) return e;
     const uint32_t npx = F.width * F.height;
-    shade_kernel<<<(npx + 255u) / 256u, 256, 0, s>>>(F);
+    if (F.flat_shade) shade_kernel<true><<<(npx + 255u) / 256u, 256, 0, s>>>(F);
+    else shade_kernel<false><<<(npx + 255u) / 256u, 256, 0, s>>>(F);
     return cudaGetLastError();
 }
 
@@ -741,11 +571,12 @@ cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s
     if (B.num_scenes == 0) return cudaSuccess;
     batch_reset_kernel<<<(B.num_scenes + 255u) / 256u, 256, 0, s>>>(B);
     if (L.tri_blocks) batch_setup_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
-    batch_scan_kernel<<<B.num_scenes, 1024, 0, s>>>(B);
+    cudaError_t e = launch_scan(L.scan, s);
+    if (e != cudaSuccess) return e;
     if (L.tri_blocks) batch_fill_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
     FrameDev none;
     memset(&none, 0, sizeof none);
-    cudaError_t e = launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, raster_smem_bytes(L.bin_w, L.bin_h), s);
+    e = launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, raster_smem_bytes(L.bin_w, L.bin_h), s);
     if (e != cudaSuccess) return e;
     if (L.px_blocks) batch_shade_kernel<<<L.px_blocks, 256, 0, s>>>(B);
     return cudaGetLastError();

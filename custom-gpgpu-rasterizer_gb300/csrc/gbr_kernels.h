@@ -11,7 +11,10 @@ cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm);
 // ctas: the raster_kernel variant compiled for 2..6 CTAs per SM (0: default)
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
 cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s);
-cudaError_t launch_scan(const FrameDev& F, bool predicted, cudaStream_t s);
+// The bin scan of a frame (mode: kScanExact, ...) and its three launches.
+ScanDev scan_of(const FrameDev& F, uint32_t mode);
+uint32_t scan_blocks(uint32_t num_bins);   // blocks of 1024 bins; FrameDev::scan_partial holds 2 per block
+cudaError_t launch_scan(const ScanDev& S, cudaStream_t s);
 cudaError_t launch_fill(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s);
 cudaError_t launch_clear(const FrameDev& F, cudaStream_t s);
@@ -23,8 +26,9 @@ struct BatchLaunch {
     uint32_t raster_grid;   // persistent raster CTAs
     uint32_t raster_ctas;   // raster variant (CTAs per SM it is compiled for; 0: default)
     uint32_t bin_w, bin_h;  // the largest bin of the batch (shared-memory tile)
+    ScanDev scan;           // the scan over the bins of every scene
 };
-// reset, setup + count, per-scene scan, fill, raster, shade: six launches
+// reset, setup + count, bin scan (three launches), fill, raster, shade
 cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s);
 cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
 

@@ -57,7 +57,8 @@ constexpr size_t kOffGvis = kOffList + align256(size_t(kNaMaxPairs) * 4u);
 constexpr size_t kOffIds = kOffGvis + align256(size_t(kNaMaxPixels) * 8u);
 constexpr size_t kOffCtl = kOffIds + align256(size_t(kNaMaxPixels) * 4u);
 constexpr size_t kOffMesh = kOffCtl + align256(sizeof(Ctl));
-constexpr size_t kScratchBytes = kOffMesh + align256(sizeof(MeshDev));
+constexpr size_t kOffPartial = kOffMesh + align256(sizeof(MeshDev));
+constexpr size_t kScratchBytes = kOffPartial + align256(size_t(2u * (kNaMaxBins / 1024u + 1u)) * 8u);
 
 // The only device memory this entry point uses besides the caller's.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -112,7 +113,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
                                          uint32_t vis, uint32_t* d_colour, float* d_depth, void* stream) {
     if (!d_vertices || !world || !cam || !d_colour || !d_depth) return na_fail(GBR_ERR_INVALID_ARG, "null argument");
     if (vertex_format > GBR_VERTEX_POS3_RGBA8 || topology > GBR_TOPOLOGY_TRIANGLE_STRIP ||
-        (!d_indices && topology != GBR_TOPOLOGY_TRIANGLE_LIST) || cull > GBR_CULL_NONE || sample > GBR_SAMPLE_LINEAR ||
+        (!d_indices && topology != GBR_TOPOLOGY_TRIANGLE_LIST) || cull > GBR_CULL_NONE || sample > GBR_SAMPLE_BILINEAR ||
         vis > GBR_VIS_NORMAL)
         return na_fail(GBR_ERR_INVALID_ARG, "bad vertex format, topology or render state");
     const uint64_t tris = !d_indices ? num_vertices / 3u
@@ -177,6 +178,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.gvis = reinterpret_cast<unsigned long long*>(b + kOffGvis);
     F.ids = reinterpret_cast<uint32_t*>(b + kOffIds);
     F.ctl = reinterpret_cast<Ctl*>(b + kOffCtl);
+    F.scan_partial = reinterpret_cast<unsigned long long*>(b + kOffPartial);
     F.colour = d_colour;
     F.depth = d_depth;
 
@@ -199,7 +201,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     if (e == cudaSuccess && ((uint64_t)num_bins_x * bin_w < width || (uint64_t)num_bins_y * bin_h < height))
         e = launch_clear(F, s);
     if (e == cudaSuccess) e = launch_setup(F, false, s);
-    if (e == cudaSuccess) e = launch_scan(F, false, s);
+    if (e == cudaSuccess) e = launch_scan(scan_of(F, kScanExact), s);
     if (e == cudaSuccess) e = launch_fill(F, s);
     if (e == cudaSuccess) e = launch_raster(F, (uint32_t)(slot.num_sms * (blocks_per_sm > 0 ? blocks_per_sm : 1)), s);
     if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));

@@ -3,17 +3,20 @@
 // Exact binning reads every triangle twice (count pass, then fill pass) with
 // one global atomic per (triangle, bin) pair in each.  Predicted binning
 // replaces the count pass:
-//   prepass_kernel   every sample_stride-th triangle goes through the vertex
-//                    stage and binning rule; per bin it accumulates the
+//   prepass_kernel   one triangle from each group of sample_stride
+//                    consecutive triangles (drawn by a hash of the group)
+//                    goes through the vertex stage and binning rule; per
+//                    bin it accumulates the
 //                    sampled pair count, and per centroid bin the count,
 //                    bounding-box area (sum, max) and depth range;
 //   capacity_kernel  12 features per bin from those accumulators -> MLP
 //                    12-64-64-1 (ReLU, softplus out; parameters BF16, math
 //                    FP32) -> predicted count l -> capacity
-//                    ceil(l*(1+alpha) + beta*sqrt(l) + gamma);
+//                    ceil(l*(1+alpha) + beta*sqrt(l+1) + gamma), at most
+//                    the triangle count;
 //   scan (capacities) -> one fused setup + fill pass appending inside each
-//                    bin's capacity -> items_kernel builds the raster work
-//                    items from the actual counts.
+//                    bin's capacity -> a scan of the filled sizes builds the
+//                    raster work items (gbr_scan.cu, kScanPredictedItems).
 // Any append beyond a bin's capacity raises ctl->pred_overflow; the exact
 // count / scan / fill kernels are always launched behind it and run only
 // then, so an overflowing frame is re-binned exactly on the device with no
@@ -23,6 +26,8 @@
 // exact count) pairs produced by exact binning; the loss is
 // (log1p(l) - log1p(count))^2.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "gbr_device.cuh"
 #include "gbr_kernels.h"
@@ -83,9 +88,25 @@ __device__ __forceinline__ float softplus(float y) { return y > 20.f ? y : log1p
 // ---------------------------------------------------------------------------
 // Frame kernels
 // ---------------------------------------------------------------------------
+// Integer hash (a 32-bit finaliser: xor-shift / multiply rounds).
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+
 __global__ void __launch_bounds__(256) prepass_kernel(FrameDev F) {
+    // one triangle drawn from each group of sample_stride consecutive
+    // triangles: a fixed stride would alias with structured index orders
+    // (a subdivided mesh numbers its children level by level, so every 8th
+    // triangle falls on a few of the base faces only)
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t prim = idx * F.sample_stride;
+    const uint32_t first = idx * F.sample_stride;
+    uint32_t prim = first + hash32(idx) % F.sample_stride;
+    if (prim >= F.num_tris) prim = first;
     const uint32_t lane = threadIdx.x & 31u;
     bool visible = false;
     int4 r = make_int4(1, 1, 0, 0);
@@ -139,19 +160,8 @@ __global__ void __launch_bounds__(256) prepass_kernel(FrameDev F) {
         atomicMin(&F.feat[4u * nb + cbin], ordered(zc));
         atomicMax(&F.feat[5u * nb + cbin], ordered(zc));
     }
-    // sampled (triangle, bin) pairs, warp-aggregated
-    bool more = visible && r.x <= r.z && r.y <= r.w;
-    int bx = r.x, by = r.y;
-    for (;;) {
-        const unsigned act = __ballot_sync(0xFFFFFFFFu, more);
-        if (!act) break;
-        if (more) {
-            const uint32_t bin = (uint32_t)bx + (uint32_t)by * F.nbx;
-            const unsigned peers = __match_any_sync(act, bin);
-            if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&F.feat[bin], (uint32_t)__popc(peers));
-            if (++bx > r.z) { bx = r.x; if (++by > r.w) more = false; }
-        }
-    }
+    // sampled (triangle, bin) pairs
+    bin_walk<3>(F, visible ? pack_rect(r, false) : empty_rect(), 0u, visible);
 }
 
 // The kFeatures features of bin b (shared by inference and training data).
@@ -170,93 +180,78 @@ __device__ __forceinline__ void bin_features(const FrameDev& F, uint32_t b, floa
     const float area_sum = __uint_as_float(__ldg(&F.feat[2u * nb + b]));
     const float area_max = __uint_as_float(__ldg(&F.feat[3u * nb + b]));
     const int tw = min((int)F.bw, (int)F.width - bx * (int)F.bw), th = min((int)F.bh, (int)F.height - by * (int)F.bh);
-    x[0] = log1pf(sc(bx, by));
-    x[1] = log1pf(n9 * (1.f / 9.f));
+    // sampled pair estimates on a linear scale (a ReLU network passes them
+    // through to the softplus output unchanged where they are right),
+    // sizes and densities on a log scale
+    const float lin = 1.f / 256.f;
+    x[0] = sc(bx, by) * lin;
+    x[1] = n9 * (1.f / 9.f) * lin;
     x[2] = log1pf((float)cc * s);
     x[3] = cc ? log1pf(area_sum / (float)cc) : 0.f;
     x[4] = cc ? log1pf(area_max) : 0.f;
     x[5] = cc ? unordered(__ldg(&F.feat[5u * nb + b])) - unordered(__ldg(&F.feat[4u * nb + b])) : 0.f;
-    x[6] = log1pf(sc(bx - 1, by));
-    x[7] = log1pf(sc(bx + 1, by));
-    x[8] = log1pf(sc(bx, by - 1));
-    x[9] = log1pf(sc(bx, by + 1));
+    x[6] = sc(bx - 1, by) * lin;
+    x[7] = sc(bx + 1, by) * lin;
+    x[8] = sc(bx, by - 1) * lin;
+    x[9] = sc(bx, by + 1) * lin;
     x[10] = (tw > 0 && th > 0) ? (float)(tw * th) / (float)(F.bw * F.bh) : 0.f;
     x[11] = log1pf((float)F.ctl->num_sampled * s / (float)nb);
+    // degenerate geometry (w near 0) can make the area or depth terms
+    // infinite: keep every feature finite
+#pragma unroll
+    for (int k = 0; k < kFeatures; ++k) x[k] = x[k] == x[k] ? fminf(fmaxf(x[k], -1.0e4f), 1.0e4f) : 0.f;
 }
 
+// One warp per bin: lane j holds hidden units j and j + 32 of both layers;
+// layer-2 inputs come from a per-warp copy of h1 in shared memory and the
+// output is a warp reduction.  Every lane returns the pre-softplus output.
+__device__ __forceinline__ float mlp_forward_warp(const float* w, const float* x, float* h1s) {
+    const uint32_t lane = threadIdx.x & 31u;
+    float a = w[kOffB1 + lane], c = w[kOffB1 + lane + 32];
+#pragma unroll
+    for (int k = 0; k < kFeatures; ++k) {
+        a = __fmaf_rn(x[k], w[kOffW1 + k * kMlpHidden + lane], a);
+        c = __fmaf_rn(x[k], w[kOffW1 + k * kMlpHidden + lane + 32], c);
+    }
+    h1s[lane] = fmaxf(a, 0.f);
+    h1s[lane + 32] = fmaxf(c, 0.f);
+    __syncwarp();
+    float p = w[kOffB2 + lane], q = w[kOffB2 + lane + 32];
+#pragma unroll 16
+    for (int i = 0; i < kMlpHidden; ++i) {
+        const float h = h1s[i];
+        p = __fmaf_rn(h, w[kOffW2 + i * kMlpHidden + lane], p);
+        q = __fmaf_rn(h, w[kOffW2 + i * kMlpHidden + lane + 32], q);
+    }
+    __syncwarp();   // h1s is reused by the warp's next bin
+    float y = __fmaf_rn(fmaxf(p, 0.f), w[kOffW3 + lane], __fmul_rn(fmaxf(q, 0.f), w[kOffW3 + lane + 32]));
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) y += __shfl_xor_sync(0xFFFFFFFFu, y, d);
+    return y + w[kOffB3];
+}
+
+// Features of every bin (and, with `predict`, the model's capacity): a
+// persistent grid of warps, one bin per warp at a time, the BF16
+// parameters expanded to FP32 in shared memory once per block.
 __global__ void __launch_bounds__(256) capacity_kernel(FrameDev F, int predict) {
     __shared__ float w[kMlpParams];
+    __shared__ float h1s[8][kMlpHidden];
     if (predict) load_params(F.mlp_w, w);
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= F.num_bins) return;
-    float x[kFeatures];
-    bin_features(F, b, x);
-    if (F.features_out)
-        for (int k = 0; k < kFeatures; ++k) F.features_out[(size_t)b * kFeatures + k] = x[k];
-    if (!predict) return;
-    float h1[kMlpHidden];
-    const float l = softplus(mlp_forward(w, x, h1));
-    const float cap = ceilf(l * (1.f + F.cap_alpha) + F.cap_beta * sqrtf(l) + F.cap_gamma);
-    F.capacity[b] = cap >= 4.0e9f ? 0xFFFFFFFFu : (uint32_t)fmaxf(cap, 0.f);
-}
-
-// After the fused setup + fill: work items from the actual per-bin counts,
-// and the pre-pass accumulators reset for the next frame.  On overflow the
-// exact kernels that follow take over.
-__global__ void __launch_bounds__(1024) items_kernel(FrameDev F) {
-    __shared__ uint32_t s_a[1024];
-    __shared__ uint32_t s_b[1024];
-    const uint32_t nb = F.num_bins;
-    const uint32_t per = (nb + blockDim.x - 1u) / blockDim.x;
-    const uint32_t b0 = threadIdx.x * per, b1 = min(b0 + per, nb);
-    for (uint32_t b = b0; b < b1; ++b) {
-        F.feat[b] = 0u;
-        F.feat[1u * nb + b] = 0u;
-        F.feat[2u * nb + b] = 0u;
-        F.feat[3u * nb + b] = 0u;
-        F.feat[4u * nb + b] = 0xFFFFFFFFu;
-        F.feat[5u * nb + b] = 0u;
-    }
-    if (F.ctl->pred_overflow) {
-        if (threadIdx.x == 0) {
-            F.ctl->num_visible = 0u;   // the exact pass counts again
-            F.ctl->num_float_path = 0u;
-        }
-        return;
-    }
-    const uint32_t chunk = F.chunk;
-    uint32_t sum = 0, items = 0;
-    for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t c = min(F.cursors[b] - F.offsets[b], F.capacity[b]);
-        sum += c;
-        items += c == 0u ? 1u : (c + chunk - 1u) / chunk;
-    }
-    s_a[threadIdx.x] = sum;
-    s_b[threadIdx.x] = items;
-    __syncthreads();
-    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
-        const uint32_t a = threadIdx.x >= off ? s_a[threadIdx.x - off] : 0u;
-        const uint32_t c = threadIdx.x >= off ? s_b[threadIdx.x - off] : 0u;
-        __syncthreads();
-        s_a[threadIdx.x] += a;
-        s_b[threadIdx.x] += c;
-        __syncthreads();
-    }
-    uint32_t item = s_b[threadIdx.x] - items;
-    const uint32_t total_items = s_b[blockDim.x - 1u];
-    const bool fits = total_items <= F.items_cap;
-    for (uint32_t b = b0; b < b1 && fits; ++b) {
-        const uint32_t c = min(F.cursors[b] - F.offsets[b], F.capacity[b]);
-        const uint32_t n = c == 0u ? 1u : (c + chunk - 1u) / chunk;
-        for (uint32_t k = 0; k < n; ++k)
-            F.items[item + k] = make_uint4(b, F.offsets[b] + k * chunk, min(chunk, c - min(c, k * chunk)), n);
-        item += n;
-    }
-    if (threadIdx.x == 0) {
-        F.ctl->num_pairs = s_a[blockDim.x - 1u];
-        F.ctl->num_items = fits ? total_items : 0u;
-        F.ctl->item_next = 0u;
-        if (!fits) F.ctl->pred_overflow = 1u;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + warp; b < F.num_bins; b += nwarps) {   // warp-uniform
+        float x[kFeatures];
+        bin_features(F, b, x);
+        if (F.features_out && lane == 0)
+            for (int k = 0; k < kFeatures; ++k) F.features_out[(size_t)b * kFeatures + k] = x[k];
+        if (!predict) continue;
+        const float l = softplus(mlp_forward_warp(w, x, h1s[warp]));
+        if (lane != 0) continue;
+        const float cap = ceilf(l * (1.f + F.cap_alpha) + F.cap_beta * sqrtf(l + 1.f) + F.cap_gamma);
+        // a bin never holds more than every triangle; an undefined prediction
+        // gets that bound too
+        const float most = (float)F.num_tris;
+        F.capacity[b] = (uint32_t)(cap == cap ? fminf(fmaxf(cap, 0.f), most) : most);
     }
 }
 
@@ -397,14 +392,12 @@ cudaError_t launch_prepass(const FrameDev& F, cudaStream_t s) {
 }
 
 cudaError_t launch_capacity(const FrameDev& F, bool predict, cudaStream_t s) {
-    capacity_kernel<<<(F.num_bins + 255u) / 256u, 256, 0, s>>>(F, predict ? 1 : 0);
+    // 8 warps per block, about four bins per warp, at most 1024 blocks
+    const uint32_t blocks = std::min<uint32_t>((F.num_bins + 31u) / 32u, 1024u);
+    capacity_kernel<<<blocks ? blocks : 1u, 256, 0, s>>>(F, predict ? 1 : 0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_items(const FrameDev& F, cudaStream_t s) {
-    items_kernel<<<1, 1024, 0, s>>>(F);
-    return cudaGetLastError();
-}
 
 __global__ void feat_reset_kernel(FrameDev F) {
     const uint32_t nb = F.num_bins;

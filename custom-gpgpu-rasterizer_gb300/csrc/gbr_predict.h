@@ -25,7 +25,6 @@ constexpr uint32_t kSampleStride = 8;
 
 cudaError_t launch_prepass(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_capacity(const FrameDev& F, bool predict, cudaStream_t s);
-cudaError_t launch_items(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_feat_reset(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_mlp_predict(const uint16_t* w, const float* x, uint32_t n, float* out, cudaStream_t s);
 cudaError_t launch_mlp_grad(const uint16_t* w, const float* x, const float* y, uint32_t n, float* grad, float* loss,

@@ -30,7 +30,7 @@ BINNING_EXACT, BINNING_PREDICTED = 0, 1
 
 EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "gbr_mesh_update_vertices",
             "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
-            "gbr_texture_upload", "gbr_texture_remove", "gbr_set_binning", "gbr_set_predictor",
+            "gbr_texture_upload", "gbr_texture_remove", "gbr_set_lights", "gbr_set_binning", "gbr_set_predictor",
             "gbr_collect_bin_features", "gbr_mlp_num_params", "gbr_mlp_predict", "gbr_mlp_loss_grad", "gbr_mlp_adam",
             "gbr_set_raster_params", "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
             "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
@@ -55,6 +55,10 @@ class Stats(C.Structure):
                 ("overflow_reruns", C.c_uint32), ("predicted_overflow", C.c_uint32),
                 ("predicted_capacity", C.c_uint64),
                 ("ms_setup", C.c_float), ("ms_bin", C.c_float), ("ms_raster", C.c_float), ("ms_total", C.c_float)]
+
+
+class Light(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("colour", C.c_float * 3), ("intensity", C.c_float), ("vec", C.c_float * 3)]
 
 
 class BatchConfig(C.Structure):
@@ -96,6 +100,7 @@ def lib():
             "gbr_scene_clear": [vp],
             "gbr_texture_upload": [vp, vp, u32, u32, C.POINTER(i32)],
             "gbr_texture_remove": [vp, i32],
+            "gbr_set_lights": [vp, vp, u32],
             "gbr_set_binning": [vp, u32],
             "gbr_set_predictor": [vp, vp, u32, C.c_float, C.c_float, C.c_float],
             "gbr_collect_bin_features": [vp, C.POINTER(Camera), u32, u32, u32, vp, vp, vp],
@@ -241,6 +246,18 @@ class Renderer:
         for m in scene.meshes:
             tex_ids = [self.add_texture(t) if t is not None else -1 for t in m.textures]
             self.add_mesh(m.vertices, m.vertex_format, m.indices, m.topology, m.world, tex_ids)
+        self.set_lights(getattr(scene, "lights", []) or [])
+
+    def set_lights(self, lights):
+        """Scene lights (objects with type, colour, intensity, vec); empty:
+        the reference shader's constant light."""
+        arr = (Light * max(len(lights), 1))()
+        for k, lt in enumerate(lights):
+            arr[k].type = int(lt.type)
+            arr[k].colour[:] = [float(x) for x in lt.colour]
+            arr[k].intensity = float(lt.intensity)
+            arr[k].vec[:] = [float(x) for x in lt.vec]
+        check(self._lib.gbr_set_lights(self.h, C.cast(arr, C.c_void_p) if lights else None, len(lights)))
 
     def set_binning(self, method: int):
         check(self._lib.gbr_set_binning(self.h, method))

@@ -24,6 +24,8 @@ VERTEX_POS3_RGBA8 = 1
 
 CULL_BACKFACE, CULL_FRONTFACE, CULL_NONE = 0, 1, 2
 SAMPLE_POINT, SAMPLE_LINEAR = 0, 1
+SAMPLE_BILINEAR = 2   # the build's extension: true bilinear filtering
+LIGHT_DIRECTIONAL, LIGHT_POINT = 0, 1
 VIS_PBR, VIS_DEPTH, VIS_NORMAL = 0, 1, 2
 TOPOLOGY_LIST, TOPOLOGY_STRIP = 0, 1
 
@@ -56,6 +58,17 @@ class Mesh:
 
 
 @dataclasses.dataclass
+class Light:
+    """A scene light (DirectionalLight / PointLight of the reference's scene
+    graph): vec is the direction the light travels, or the point light's
+    world position."""
+    type: int
+    colour: tuple
+    intensity: float
+    vec: tuple
+
+
+@dataclasses.dataclass
 class Camera:
     pos: np.ndarray   # (3,) f32
     fwd: np.ndarray   # (3,) f32
@@ -76,6 +89,7 @@ class Scene:
     sample: int = SAMPLE_POINT
     vis: int = VIS_PBR
     seed: int = 0
+    lights: List[Light] = dataclasses.field(default_factory=list)   # empty: the shader's constant light
 
     @property
     def num_bins_x(self) -> int:
@@ -390,3 +404,15 @@ def icosphere_scene(width: int = 3840, height: int = 2160, bin_size: int = 16, s
     cam = perspective_camera((0.0, 0.0, distance), 60.0, width, height)
     return Scene(f"icosphere{subdiv}", width, height, bin_size, bin_size, cam, [mesh], cull=CULL_BACKFACE,
                  sample=sample, vis=vis)
+
+
+def icosphere_lit_scene(width: int = 3840, height: int = 2160, bin_size: int = 16, subdiv: int = 7,
+                        tex_size: int = 2048, distance: float = 8.0) -> Scene:
+    """The displaced icosphere with the build's shading extensions: bilinear
+    filtering of the 2048^2 noise texture, one directional and one point
+    light (the reference's GPU shader has neither)."""
+    s = icosphere_scene(width, height, bin_size, subdiv, tex_size, distance, sample=SAMPLE_BILINEAR)
+    s.name = f"icosphere{subdiv}_lit"
+    s.lights = [Light(LIGHT_DIRECTIONAL, (1.0, 0.95, 0.9), 4.0, (0.577, -0.577, -0.577)),
+                Light(LIGHT_POINT, (0.4, 0.6, 1.0), 30.0, (2.0, 1.5, 3.0))]
+    return s

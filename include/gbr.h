@@ -35,8 +35,11 @@ typedef enum {
 
 /* CullingMode (CullingMode.h:3-7) */
 enum { GBR_CULL_BACKFACE = 0, GBR_CULL_FRONTFACE = 1, GBR_CULL_NONE = 2 };
-/* SampleState (SampleState.h:3-7) */
-enum { GBR_SAMPLE_POINT = 0, GBR_SAMPLE_LINEAR = 1 };
+/* SampleState (SampleState.h:3-7); GBR_SAMPLE_BILINEAR is the build's
+ * extension (the reference's "Linear" is a 5-tap filter,
+ * CUDATextureSampler.cuh:112-190): true bilinear filtering, texel centres at
+ * (i + 1/2) / size, addresses clamped to the texture. */
+enum { GBR_SAMPLE_POINT = 0, GBR_SAMPLE_LINEAR = 1, GBR_SAMPLE_BILINEAR = 2 };
 /* VisualisationState (VisualisationState.h:3-7) */
 enum { GBR_VIS_PBR = 0, GBR_VIS_DEPTH = 1, GBR_VIS_NORMAL = 2 };
 /* PrimitiveTopology (PrimitiveTopology.h:3-7) */
@@ -123,7 +126,8 @@ gbr_status gbr_texture_remove(gbr_renderer *r, int32_t tex_id);
  * fixed size and drop triangles when full, CUDAAtomicQueue.cuh:8-26).
  * gbr_set_predictor installs the capacity model: num_params BF16 parameters
  * of the 12-64-64-1 MLP (gbr_mlp_num_params()) and the capacity rule
- * ceil(l*(1+alpha) + beta*sqrt(l) + gamma) for a predicted count l.  With
+ * ceil(l*(1+alpha) + beta*sqrt(l+1) + gamma) for a predicted count l,
+ * clamped to the scene's triangle count.  With
  * GBR_BINNING_PREDICTED a frame bins in one pass into the predicted
  * capacities; if any bin overflows, the frame is re-binned exactly on the
  * device, so bin lists and images never depend on the prediction.
@@ -143,6 +147,25 @@ gbr_status gbr_mlp_loss_grad(const uint16_t *d_w, const float *d_x, const float 
                              float *d_loss, void *stream);
 gbr_status gbr_mlp_adam(float *d_master, uint16_t *d_w, const float *d_grad, float *d_m, float *d_v, uint32_t step,
                         float lr, float grad_scale, void *stream);
+
+/* Scene lights (SceneGraph::AddLight with DirectionalLight / PointLight,
+ * SceneGraph.h, DirectionalLight.cpp, PointLight.cpp).  The reference's GPU
+ * shader ignores the scene's lights and uses one constant light
+ * (CUDAROPs.cu:417-420); that stays the behaviour with no lights set.  With
+ * n > 0 lights the normal-mapped shading sums, per light, the shader's
+ * Lambert (and, with specular and gloss maps, Phong) terms with L = the
+ * direction the light travels at the shaded world point and irradiance =
+ * colour x intensity (/ squared distance for a point light), plus the
+ * shader's ambient and MaxToOne.  Up to 8 lights; n = 0 restores the
+ * constant light. */
+enum { GBR_LIGHT_DIRECTIONAL = 0, GBR_LIGHT_POINT = 1 };
+typedef struct {
+    uint32_t type;     /* GBR_LIGHT_* */
+    float colour[3];
+    float intensity;
+    float vec[3];      /* directional: direction the light travels; point: world position */
+} gbr_light;
+gbr_status gbr_set_lights(gbr_renderer *r, const gbr_light *lights, uint32_t n);
 
 /* Binning method for the following frames. */
 gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);

@@ -185,6 +185,7 @@ typedef struct {
     float p[4];        /* NDC xyz, clip w */
     v2 uv;
     v3 n, tan, vd, c;
+    v3 wp;             /* world position (scene lights) */
 } overtex;
 
 typedef struct {
@@ -230,6 +231,7 @@ static void vs_full(const mesh_state *ms, const orc_frame *f, uint32_t vi, overt
     orc_vs_position(ms->m->world, iv, wp);
     const v3 wpos = {wp[0], wp[1], wp[2]}, cp = {f->cam_pos[0], f->cam_pos[1], f->cam_pos[2]};
     o->vd = normalize3(sub3(wpos, cp));
+    o->wp = wpos;
     o->uv.x = iv[3]; o->uv.y = iv[4];
     o->c.x = iv[11]; o->c.y = iv[12]; o->c.z = iv[13];
 }
@@ -531,8 +533,35 @@ static v3 sample_linear(const uint32_t *px, uint32_t w, uint32_t h, v2 uv)
     return out;
 }
 
+/* Bilinear filtering (the build's extension; the reference's "linear"
+ * sampler is the 5-tap filter above): texel centres at (i + 1/2) / size,
+ * the four nearest texels weighted by the fractional offsets, addresses
+ * clamped to the texture. */
+static v3 sample_bilinear(const uint32_t *px, uint32_t w, uint32_t h, v2 uv)
+{
+    const float x = fmaf(uv.x, (float)w, -0.5f), y = fmaf(uv.y, (float)h, -0.5f);
+    const float fx = floorf(x), fy = floorf(y);
+    const float ax = x - fx, ay = y - fy;
+    int xi = cvt_s32(fx), yi = cvt_s32(fy);
+    xi = xi < -1 ? -1 : (xi > (int)w - 1 ? (int)w - 1 : xi);
+    yi = yi < -1 ? -1 : (yi > (int)h - 1 ? (int)h - 1 : yi);
+    const uint32_t x0 = (uint32_t)(xi < 0 ? 0 : xi), x1 = (uint32_t)(xi + 1 > (int)w - 1 ? (int)w - 1 : xi + 1);
+    const uint32_t y0 = (uint32_t)(yi < 0 ? 0 : yi), y1 = (uint32_t)(yi + 1 > (int)h - 1 ? (int)h - 1 : yi + 1);
+    const uint32_t c00 = px[x0 + y0 * w], c10 = px[x1 + y0 * w], c01 = px[x0 + y1 * w], c11 = px[x1 + y1 * w];
+    float out[3];
+    for (int k = 0; k < 3; ++k) {
+        const float a = (float)((c00 >> (8 * k)) & 0xFFu), b = (float)((c10 >> (8 * k)) & 0xFFu);
+        const float c = (float)((c01 >> (8 * k)) & 0xFFu), d = (float)((c11 >> (8 * k)) & 0xFFu);
+        const float top = fmaf(ax, b - a, a), bottom = fmaf(ax, d - c, c);
+        out[k] = fmaf(ay, bottom - top, top) * (1.0f / 255.f);
+    }
+    v3 o = {out[0], out[1], out[2]};
+    return o;
+}
+
 static v3 sample_tex(const uint32_t *px, uint32_t w, uint32_t h, v2 uv, uint32_t ss)
 {
+    if (ss == 2u) return sample_bilinear(px, w, h, uv);
     return ss == 1u ? sample_linear(px, w, h, uv) : sample_point(px, w, h, uv);
 }
 
@@ -552,7 +581,62 @@ uint32_t orc_rgba_from_colour(const float *rgb)
     return r8 | (g8 << 8) | (b8 << 16);
 }
 
-static v3 shade_pixel_safe(const orc_mesh *m, v2 uv, v3 n, v3 tan, v3 vd, uint32_t ss)
+/* Lambert + Phong over the scene lights (the build's extension, used when
+ * lights are set): per light the reference shader's terms with its constant
+ * light replaced -- L = the direction the light travels at P (a point
+ * light's from its position to P), irradiance E = intensity (/ squared
+ * distance for a point light), diffuse += diffuse * colour * max(0,
+ * dot(-N, L)) / pi * E, specular += specular * colour * clamp(dot(vd,
+ * reflect(L, N)), 0, 1)^(gloss * 25); then ambient + diffuse + specular and
+ * MaxToOne as CUDAROPs.cu:452-455, or the diffuse term alone without the
+ * specular and gloss maps (:459-462). */
+static v3 shade_lit(const orc_frame *f, v3 diffuse, v3 fn, v3 vd, v3 P, int has_spec, v3 spec, v3 gloss)
+{
+    v3 dacc = {0.f, 0.f, 0.f}, sacc = {0.f, 0.f, 0.f};
+    const v3 nfn = {-fn.x, -fn.y, -fn.z};
+    for (uint32_t k = 0; k < f->num_lights && k < ORC_MAX_LIGHTS; ++k) {
+        const orc_light *lt = &f->lights[k];
+        v3 L;
+        float E;
+        if (lt->type == ORC_LIGHT_POINT) {
+            const v3 d = {P.x - lt->vec[0], P.y - lt->vec[1], P.z - lt->vec[2]};
+            E = lt->intensity / dot3(d, d);
+            L = normalize3(d);
+        } else {
+            L.x = lt->vec[0]; L.y = lt->vec[1]; L.z = lt->vec[2];
+            E = lt->intensity;
+        }
+        float obs = dot3(nfn, L);
+        obs = obs > 0.f ? obs : 0.f;
+        obs = obs / (float)3.14159265358979323846;
+        obs = obs * E;
+        dacc.x = fmaf(diffuse.x * lt->colour[0], obs, dacc.x);
+        dacc.y = fmaf(diffuse.y * lt->colour[1], obs, dacc.y);
+        dacc.z = fmaf(diffuse.z * lt->colour[2], obs, dacc.z);
+        if (has_spec) {
+            const float s2 = 2.f * dot3(L, fn);
+            const v3 refl = {fmaf(fn.x, s2, -L.x), fmaf(fn.y, s2, -L.y), fmaf(fn.z, s2, -L.z)};
+            float ang = dot3(vd, refl);
+            ang = ang < 0.f ? 0.f : (ang > 1.f ? 1.f : ang);
+            ang = powf(ang, gloss.x * 25.f);
+            sacc.x = fmaf(spec.x * lt->colour[0], ang, sacc.x);
+            sacc.y = fmaf(spec.y * lt->colour[1], ang, sacc.y);
+            sacc.z = fmaf(spec.z * lt->colour[2], ang, sacc.z);
+        }
+    }
+    if (!has_spec) return dacc;
+    v3 fc = {0.05f + dacc.x, 0.05f + dacc.y, 0.05f + dacc.z};
+    fc.x = fc.x + sacc.x; fc.y = fc.y + sacc.y; fc.z = fc.z + sacc.z;
+    float mx = fc.y < fc.z ? fc.z : fc.y;
+    mx = fc.x < mx ? mx : fc.x;
+    if (mx > 1.f) {
+        const float rev = 1.0f / mx;
+        fc.x *= rev; fc.y *= rev; fc.z *= rev;
+    }
+    return fc;
+}
+
+static v3 shade_pixel_safe(const orc_frame *f, const orc_mesh *m, v2 uv, v3 n, v3 tan, v3 vd, v3 P, uint32_t ss)
 {
     const v3 amb = {0.05f, 0.05f, 0.05f};
     const v3 L = {0.577f, -0.577f, -0.577f};
@@ -567,6 +651,13 @@ static v3 shade_pixel_safe(const orc_mesh *m, v2 uv, v3 n, v3 tan, v3 vd, uint32
     fn.x = fmaf(n.x, fn0.z, fmaf(tan.x, fn0.x, bin.x * fn0.y));
     fn.y = fmaf(n.y, fn0.z, fmaf(tan.y, fn0.x, bin.y * fn0.y));
     fn.z = fmaf(n.z, fn0.z, fmaf(tan.z, fn0.x, bin.z * fn0.y));
+    if (f->num_lights) {
+        const int has_spec = m->tex[2] && m->tex[3];
+        const v3 zero = {0.f, 0.f, 0.f};
+        const v3 spec = has_spec ? sample_tex(m->tex[2], m->tex_w[2], m->tex_h[2], uv, ss) : zero;
+        const v3 gloss = has_spec ? sample_tex(m->tex[3], m->tex_w[3], m->tex_h[3], uv, ss) : zero;
+        return shade_lit(f, diffuse, fn, vd, P, has_spec, spec, gloss);
+    }
     const v3 nfn = {-fn.x, -fn.y, -fn.z};
     float obs = dot3(nfn, L);
     {   /* ClampFast(obs, 0, obs) (CUDAROPs.cu:439): a no-op for obs < 0 */
@@ -632,8 +723,14 @@ static uint32_t shade_fragment(const orc_frame *f, const mesh_state *ms, const t
                     INTERP(v[0].tan.z, v[1].tan.z, v[2].tan.z)};
     const v3 vd = normalize3((v3){INTERP(v[0].vd.x, v[1].vd.x, v[2].vd.x), INTERP(v[0].vd.y, v[1].vd.y, v[2].vd.y),
                                   INTERP(v[0].vd.z, v[1].vd.z, v[2].vd.z)});
+    v3 P = {0.f, 0.f, 0.f};
+    if (f->num_lights) {   /* world position, perspective-correct like uv */
+        P.x = INTERP(v[0].wp.x, v[1].wp.x, v[2].wp.x) * winterp;
+        P.y = INTERP(v[0].wp.y, v[1].wp.y, v[2].wp.y) * winterp;
+        P.z = INTERP(v[0].wp.z, v[1].wp.z, v[2].wp.z) * winterp;
+    }
 #undef INTERP
-    const v3 col = shade_pixel_safe(m, uv, n, tan, vd, f->sample);
+    const v3 col = shade_pixel_safe(f, m, uv, n, tan, vd, P, f->sample);
     const float rgb[3] = {col.x, col.y, col.z};
     return orc_rgba_from_colour(rgb);
 }

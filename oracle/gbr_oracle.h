@@ -29,11 +29,25 @@ extern "C" {
 #define ORC_RASTER_REFERENCE   0u  /* float edge functions at integer pixels (CUDAROPs.cu:128-145) */
 #define ORC_RASTER_FIXED       1u  /* the GB300 build's 16.16 fixed-point edge functions */
 
+/* Scene lights (the build's extension; the reference's GPU shader has one
+ * constant light, CUDAROPs.cu:417-420).  Light colour x intensity as
+ * DirectionalLight::GetBiradiance, / squared distance for a point light as
+ * PointLight::GetBiradiance (DirectionalLight.cpp, PointLight.cpp). */
+#define ORC_MAX_LIGHTS         8u
+#define ORC_LIGHT_DIRECTIONAL  0u  /* vec = direction the light travels */
+#define ORC_LIGHT_POINT        1u  /* vec = world position */
+typedef struct {
+    uint32_t type;
+    float colour[3];
+    float intensity;
+    float vec[3];
+} orc_light;
+
 typedef struct {
     uint32_t width, height;
     uint32_t num_bins_x, num_bins_y, bin_w, bin_h;
     uint32_t cull;          /* 0 BackFace, 1 FrontFace, 2 NoCulling */
-    uint32_t sample;        /* 0 Point, 1 Linear */
+    uint32_t sample;        /* 0 Point, 1 Linear, 2 Bilinear (the build's extension) */
     uint32_t vis;           /* 0 PBR, 1 Depth, 2 Normal */
     uint32_t raster_mode;   /* ORC_RASTER_* */
     uint32_t clear_colour32;
@@ -44,6 +58,8 @@ typedef struct {
     float cam_fwd[3];
     float view[16];         /* column-major, element (r,c) at [c*4+r] */
     float proj[16];
+    uint32_t num_lights;    /* 0: the reference shader's constant light */
+    orc_light lights[ORC_MAX_LIGHTS];
 } orc_frame;
 
 typedef struct {

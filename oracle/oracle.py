@@ -16,6 +16,13 @@ RASTER_REFERENCE = 0
 RASTER_FIXED = 1
 
 
+MAX_LIGHTS = 8
+
+
+class OrcLight(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("colour", C.c_float * 3), ("intensity", C.c_float), ("vec", C.c_float * 3)]
+
+
 class OrcFrame(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32),
                 ("num_bins_x", C.c_uint32), ("num_bins_y", C.c_uint32),
@@ -24,7 +31,8 @@ class OrcFrame(C.Structure):
                 ("raster_mode", C.c_uint32), ("clear_colour32", C.c_uint32), ("num_threads", C.c_uint32),
                 ("bin_stride", C.c_uint32), ("bin_phase", C.c_uint32),
                 ("cam_pos", C.c_float * 3), ("cam_fwd", C.c_float * 3),
-                ("view", C.c_float * 16), ("proj", C.c_float * 16)]
+                ("view", C.c_float * 16), ("proj", C.c_float * 16),
+                ("num_lights", C.c_uint32), ("lights", OrcLight * MAX_LIGHTS)]
 
 
 class OrcMesh(C.Structure):
@@ -89,6 +97,15 @@ class _Prepared:
         f.cam_fwd[:] = [float(x) for x in cam.fwd]
         f.view[:] = [float(x) for x in cam.view]
         f.proj[:] = [float(x) for x in cam.proj]
+        lights = list(getattr(scene, "lights", []) or [])
+        if len(lights) > MAX_LIGHTS:
+            raise ValueError(f"at most {MAX_LIGHTS} lights")
+        f.num_lights = len(lights)
+        for k, lt in enumerate(lights):
+            f.lights[k].type = lt.type
+            f.lights[k].colour[:] = [float(x) for x in lt.colour]
+            f.lights[k].intensity = float(lt.intensity)
+            f.lights[k].vec[:] = [float(x) for x in lt.vec]
         self.frame = f
         self.keep = []
         meshes = (OrcMesh * max(len(scene.meshes), 1))()

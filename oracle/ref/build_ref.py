@@ -77,7 +77,34 @@ PATCHES = [
      "\t\t\tdev_DepthMutexBuffer[pixelIdx] = 0;\n\t\t\t//end of critical section\n\t\t}\n\t} while (!isDone && ++spinGuard < (1u << 26));", False),
     # P9
     ("CUDARenderer.h", "private:", "public:", "all"),
+    # E1-E4: the CPU renderer (ERenderer.cpp, absent from the reference's
+    # project) against the current Mesh / SceneManager API: raw vertex and
+    # index buffers, GetNum* counts, GetWorldConst, the visualisation state
+    # instead of IsDepthColour, textures looked up by the harness
+    ("ERenderer.cpp", "\t\tconst std::vector<IVertex>& vertexBuffer = pMesh->GetVertexBuffer();\n"
+                      "\t\tconst unsigned int numVertices = pMesh->GetVertexAmount();\n"
+                      "\t\tconst std::vector<unsigned int>& indexBuffer = pMesh->GetIndexBuffer();\n"
+                      "\t\tconst unsigned int numIndices = pMesh->GetIndexAmount();\n"
+                      "\t\tm_pTextures = &pMesh->GetTextures();",
+     "\t\tconst IVertex* vertexBuffer = pMesh->GetVertexBuffer();\n"
+     "\t\tconst unsigned int numVertices = pMesh->GetNumVertices();\n"
+     "\t\tconst unsigned int* indexBuffer = pMesh->GetIndexBuffer();\n"
+     "\t\tconst unsigned int numIndices = pMesh->GetNumIndices();\n"
+     "\t\tm_pTextures = &ErefTexturesOf(pMesh);", False),                                           # E1
+    ("ERenderer.cpp", "GetNDCMeshVertices(vertexBuffer, viewProjectionMatrix, pMesh->GetWorldMatrix())",
+     "GetNDCMeshVertices(reinterpret_cast<const float*>(vertexBuffer), numVertices, viewProjectionMatrix, "
+     "pMesh->GetWorldConst())", False),                                                               # E2
+    ("ERenderer.cpp", "!sm.IsDepthColour()", "!(sm.GetVisualisationState() == VisualisationState::Depth)", "all"),  # E3
+    ("ERenderer.cpp", '#include "CullingMode.h"\n',
+     '#include "CullingMode.h"\n#include "VisualisationState.h"\n#include "SampleState.h"\n'
+     "const Textures& ErefTexturesOf(const Mesh* pMesh);\n", False),                                # E4
+    ("SceneManager.h", "private:", "public:", "all"),                                                  # E5
+    ("ERenderer.h", "\tprivate:", "\tpublic:", "all"),                                                 # E6
 ]
+
+ERENDERER_SOURCES = ["ERenderer.cpp", "Mesh.cpp", "SceneGraph.cpp", "SceneManager.cpp", "Camera.cpp", "Texture.cpp",
+                     "Light.cpp", "DirectionalLight.cpp", "PointLight.cpp", "EventManager.cpp"]
+EREF_BIN = os.path.join(OUT, "eref_harness")
 
 
 def _apply(text, pat, rep, mode, name):
@@ -145,7 +172,30 @@ def build(force: bool = False) -> str:
     return BIN
 
 
+def build_erenderer(force: bool = False) -> str:
+    """Compile oracle/ref/eref_harness.cpp with the reference's CPU renderer
+    (ERenderer.cpp and the scene classes it uses, staged and patched E1-E5)
+    and headless SDL stand-ins into oracle/_ref/eref_harness, with g++ at
+    -O2 and no floating-point contraction (the reference's MSVC build does
+    not fuse)."""
+    if not os.path.isdir(SRC):
+        stage()
+    inputs = [os.path.join(HERE, "eref_harness.cpp"), os.path.join(HERE, "eref_stubs.cpp"), os.path.join(SRC, ".staged")]
+    if not force and os.path.exists(EREF_BIN) and all(os.path.getmtime(EREF_BIN) >= os.path.getmtime(i) for i in inputs):
+        return EREF_BIN
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    inc = ["-I", SRC, "-I", os.path.join(SRC, "sdl", "sdl2-2.0.9"), "-I", os.path.join(SRC, "sdl", "sdl2_image-2.0.5"),
+           "-I", cuda_inc]
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-w", "-ffp-contract=off", "-include", "cstring", *inc,
+           os.path.join(HERE, "eref_harness.cpp"), os.path.join(HERE, "eref_stubs.cpp"),
+           *[os.path.join(SRC, f) for f in ERENDERER_SOURCES], "-lpthread", "-o", EREF_BIN + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(EREF_BIN + ".tmp", EREF_BIN)
+    return EREF_BIN
+
+
 if __name__ == "__main__":
     if "--stage" in sys.argv or os.path.isdir(CCR):
         stage(force="--force" in sys.argv)
     print(build(force="--force" in sys.argv))
+    print(build_erenderer(force="--force" in sys.argv))

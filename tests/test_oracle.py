@@ -150,6 +150,46 @@ def test_linear_sampler_is_five_tap_cross_with_row_wrap():
     assert got[0] == np.float32(r * np.float32(np.float32(1) / np.float32(255)))
 
 
+def test_bilinear_extension_weights_and_clamping():
+    tex = np.array([[0, 100], [40, 200]], np.uint32)   # red channel
+    # texel centres reproduce the texels
+    assert oracle.sample(tex, 0.25, 0.25, 2)[0] == 0.0
+    assert np.isclose(oracle.sample(tex, 0.75, 0.25, 2)[0], 100 / 255, atol=1e-7)
+    assert np.isclose(oracle.sample(tex, 0.25, 0.75, 2)[0], 40 / 255, atol=1e-7)
+    # the midpoint averages all four
+    assert np.isclose(oracle.sample(tex, 0.5, 0.5, 2)[0], (0 + 100 + 40 + 200) / 4 / 255, atol=1e-6)
+    # a quarter of the way from texel (0,0) to (1,0) along x, on row 0
+    assert np.isclose(oracle.sample(tex, 0.375, 0.25, 2)[0], 25 / 255, atol=1e-6)
+    # outside [0, 1] clamps to the edge texels (no magenta)
+    assert np.isclose(oracle.sample(tex, -3.0, 0.25, 2)[0], 0.0, atol=1e-7)
+    assert np.isclose(oracle.sample(tex, 7.0, 9.0, 2)[0], 200 / 255, atol=1e-7)
+
+
+def test_scene_lights_extension_in_the_oracle():
+    """No lights: the reference's constant light.  A directional light
+    against the viewer darkens the lit side; a point light adds falloff."""
+    base = scenes.sphere_scene(160, 120)
+    a = oracle.render(base, oracle.RASTER_FIXED, want_bins=False)
+    lit = scenes.sphere_scene(160, 120)
+    lit.lights = [scenes.Light(scenes.LIGHT_DIRECTIONAL, (1.0, 1.0, 1.0), 7.0, (0.577, -0.577, -0.577))]
+    b = oracle.render(lit, oracle.RASTER_FIXED, want_bins=False)
+    assert np.array_equal(a["ids"], b["ids"]) and np.array_equal(a["depth"], b["depth"])
+    # same light as the constant one: identical wherever the Lambert term is
+    # non-negative (the constant light keeps negative terms, CUDAROPs.cu:439)
+    cov = a["ids"] != 0xFFFFFFFF
+    same = (a["colour"] == b["colour"]) & cov
+    assert same.sum() > 0.4 * cov.sum()
+    pt = scenes.sphere_scene(160, 120)
+    pt.lights = [scenes.Light(scenes.LIGHT_POINT, (1.0, 1.0, 1.0), 20.0, (0.0, 0.0, 2.5))]
+    c = oracle.render(pt, oracle.RASTER_FIXED, want_bins=False)
+    ch = lambda x: (x >> 8) & 255
+    # the point light sits in front of the sphere: the centre is brighter than the rim
+    cy, cx = 60, 80
+    centre = ch(c["colour"][cy, cx].astype(np.int64))
+    rim_x = cx + int(np.argmax(~cov[cy, cx:])) - 2
+    assert centre > ch(c["colour"][cy, rim_x].astype(np.int64))
+
+
 def test_rgba_swizzle_and_truncation():
     # GetRGBAFromColour: r8 = b*255, g8 = g*255, b8 = r*255, truncating
     c = oracle.rgba_from_colour([1.0, 0.5, 0.25])

@@ -234,6 +234,28 @@ def test_icosphere_4k_subpixel(gbr_lib, cuda_device, bins):
     assert g["stats"]["num_visible"] > 100_000 and (g["ids"] != EMPTY).sum() > 100_000
 
 
+@pytest.mark.parametrize("lights", [False, True])
+def test_bilinear_and_scene_lights_extension(gbr_lib, cuda_device, lights):
+    """The build's shading extensions (true bilinear filtering, directional
+    and point scene lights; the reference's GPU shader has neither) against
+    the oracle, which restates them."""
+    s = scenes.sphere_scene(320, 240, sample=scenes.SAMPLE_BILINEAR)
+    if lights:
+        s.lights = [scenes.Light(scenes.LIGHT_DIRECTIONAL, (1.0, 0.9, 0.8), 5.0, (0.577, -0.577, -0.577)),
+                    scenes.Light(scenes.LIGHT_POINT, (0.3, 0.5, 1.0), 12.0, (1.2, 0.8, 2.0))]
+    g, o = run_case(gbr_lib, s, ref_band=False)
+    assert len(np.unique(g["colour"])) > 500
+
+
+def test_lit_icosphere_bilinear(gbr_lib, cuda_device):
+    """The displaced icosphere with bilinear filtering of its noise texture and
+    a directional plus a point light (smaller than 4K so the oracle stays
+    quick)."""
+    s = scenes.icosphere_lit_scene(960, 540, subdiv=6, tex_size=1024, distance=3.0)
+    g, o = run_case(gbr_lib, s, ref_band=False)
+    assert (g["ids"] != EMPTY).sum() > 10_000
+
+
 def test_full_size_soup_1m_1080p(gbr_lib, cuda_device):
     """1M-triangle 1920x1080 soup: bin lists bit-exact at full size; the raster
     checked exactly against the oracle on every 53rd bin."""

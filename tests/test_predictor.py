@@ -99,8 +99,12 @@ def _constant_model(count: float) -> np.ndarray:
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("count,expect_overflow", [(40000.0, False), (2.0, True)])
+@pytest.mark.parametrize("count,expect_overflow", [(4000.0, False), (2.0, True), (5.0e6, True)])
 def test_predicted_binning_is_identical_to_exact(gbr_lib, cuda_device, count, expect_overflow):
+    """Capacities that hold, capacities that overflow a bin, and predictions
+    whose capacities add up to far more than the bin storage (5e6 per bin,
+    6e9 before clamping to the triangle count): the frame is re-binned
+    exactly on the device and matches exact binning."""
     s = scenes.soup_scene(60000, 640, 480, seed=41)
     exact = _frame(gbr_lib, s)
     pred = _frame(gbr_lib, s, (_constant_model(count), 0.0, 0.0, 0.0))
