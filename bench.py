@@ -191,6 +191,45 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def predicted_binning(r, scene, args, stream, flush):
+    """The same device-resident frame with learned-capacity binning (the
+    committed model): time per frame, binning time, frame overflow rate and
+    over-allocation of the predicted capacities, against exact binning on
+    the same renderer."""
+    import torch
+    import gbr
+    import predictor
+
+    if not os.path.exists(predictor.WEIGHTS):
+        return None
+    sptr = stream.cuda_stream
+    predictor.install(r)
+    out = {"ms_per_step": [], "ms_binning": [], "overflow": 0, "over_allocation": []}
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            r.render_scene(scene, sptr)
+            r.stats(sptr)
+        for total_only in (False, True):
+            r.set_timing(True, total_only=total_only)
+            for _ in range(args.steps):
+                flush.zero_()
+                r.render_scene(scene, sptr)
+                st = r.stats(sptr)
+                if total_only:
+                    out["ms_per_step"].append(st["ms_total"])
+                else:
+                    out["ms_binning"].append(st["ms_setup"] + st["ms_bin"])
+                out["overflow"] += int(st["predicted_overflow"])
+                out["over_allocation"].append(st["predicted_capacity"] / max(st["num_pairs"], 1) - 1.0)
+    r.set_binning(gbr.BINNING_EXACT)
+    r.set_timing(True)
+    t = statistics.mean(out["ms_per_step"]) / 1e3
+    return {"ms_per_step": t * 1e3, "triangles_per_s": N_TRI / t, "ms_binning": statistics.mean(out["ms_binning"]),
+            "frame_overflow_rate": out["overflow"] / (2 * args.steps),
+            "over_allocation": statistics.mean(out["over_allocation"]),
+            "model": "12-64-64-1 MLP, BF16 weights (custom-gpgpu-rasterizer_gb300/predictor_weights.npz)"}
+
+
 def run_ours(args, rank, world, local):
     import torch
     import gbr
@@ -222,18 +261,36 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize(dev)
     if dist:
         dist.barrier()
+    # stage breakdown: an event between stages (keeps launches from overlapping)
+    ms_setup, ms_bin, ms_raster, ms_shade = [], [], [], []
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            r.render_scene(scene, sptr)
+            st = r.stats(sptr)
+            ms_setup.append(st["ms_setup"]); ms_bin.append(st["ms_bin"])
+            ms_raster.append(st["ms_raster"]); ms_shade.append(st["ms_shade"])
+    # the timed frames: frame events only
+    r.set_timing(True, total_only=True)
+    with torch.cuda.stream(stream):
+        r.render_scene(scene, sptr)
+        r.stats(sptr)
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
     sampler = ClockSampler(local)
-    ms_total, ms_setup, ms_bin, ms_raster = [], [], [], []
+    ms_total = []
     torch.cuda.synchronize(dev)
     with torch.cuda.stream(stream):
         for _ in range(args.steps):
             flush.zero_()
             r.render_scene(scene, sptr)
             st = r.stats(sptr)
-            ms_total.append(st["ms_total"]); ms_setup.append(st["ms_setup"])
-            ms_bin.append(st["ms_bin"]); ms_raster.append(st["ms_raster"])
+            ms_total.append(st["ms_total"])
     torch.cuda.synchronize(dev)
     clocks = sampler.stop()
+    r.set_timing(True)
+    predicted = predicted_binning(r, scene, args, stream, flush)
     pairs = st["num_pairs"]
     t_frame = sum(ms_total) / len(ms_total) / 1e3
     if dist:
@@ -301,14 +358,15 @@ def run_ours(args, rank, world, local):
                            "l2": "256 MB write between timed frames", "pairs": int(pairs),
                            "frames_per_s": world / t_frame,
                            "ms_setup": statistics.mean(ms_setup), "ms_bin": statistics.mean(ms_bin),
-                           "ms_raster": statistics.mean(ms_raster),
-                           "frame_hbm_frac": frame_bytes / t_frame / 1e9 / peak},
+                           "ms_raster": statistics.mean(ms_raster), "ms_shade": statistics.mean(ms_shade),
+                           "frame_hbm_frac": frame_bytes / t_frame / 1e9 / peak,
+                           "predicted_binning": predicted},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": profile_traffic(), "kernel": "raster_kernel",
                              "peak_source": peak_kind, "algorithmic_bytes_per_launch": raster_bytes},
                 "e2e": {"value": world * N_TRI / t_e2e, "unit": UNIT, "h2d_bytes_per_step": vbytes,
                         "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
-                "gpu_launches": 5 * args.steps,
+                "gpu_launches": 7 * args.steps,   # setup, scan x3, fill, raster, shade
                 "clocks": clocks,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
@@ -342,7 +400,9 @@ def run_icosphere(args, rank, world, local):
             with torch.cuda.stream(stream):
                 for _ in range(args.warmup):
                     r.render_scene(s, sptr)
-                    r.stats(sptr)
+                    st = r.stats(sptr)
+                stages = st
+                r.set_timing(True, total_only=True)
                 ms = []
                 for _ in range(args.steps):
                     flush.zero_()
@@ -350,8 +410,9 @@ def run_icosphere(args, rank, world, local):
                     st = r.stats(sptr)
                     ms.append(st["ms_total"])
             per_bins[bins] = {"ms_frame": statistics.mean(ms), "pairs": int(st["num_pairs"]),
-                              "visible": int(st["num_visible"]), "ms_setup": st["ms_setup"], "ms_bin": st["ms_bin"],
-                              "ms_raster": st["ms_raster"]}
+                              "visible": int(st["num_visible"]), "ms_setup": stages["ms_setup"],
+                              "ms_bin": stages["ms_bin"], "ms_raster": stages["ms_raster"],
+                              "ms_shade": stages["ms_shade"]}
     clocks = sampler.stop()
     n_tri = s.num_triangles
     best = min(per_bins, key=lambda k: per_bins[k]["ms_frame"])
@@ -365,7 +426,7 @@ def run_icosphere(args, rank, world, local):
                                      "resolution": [3840, 2160], "best_bins": best,
                                      "bins_8x8": per_bins[8], "bins_16x16": per_bins[16],
                                      "l2": "256 MB write between timed frames"},
-                          "gpu_launches": 5 * args.steps * 2, "clocks": clocks}), flush=True)
+                          "gpu_launches": 7 * args.steps * 2, "clocks": clocks}), flush=True)
 
 
 BATCH_SCENES = 256
@@ -477,7 +538,7 @@ def run_batch(args, rank, world, local):
                            "l2": "256 MB write between timed frames"},
                 "e2e": {"value": world * n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "gpu_launches": 6 * args.steps,
+                "gpu_launches": 8 * args.steps,   # reset, setup, scan x3, fill, raster, shade
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     b.close()
@@ -489,8 +550,9 @@ def run_batch(args, rank, world, local):
     return line
 
 
-def profile_frames(n: int):
-    """The benchmark's frame, device resident, n times on the default stream."""
+def profile_frames(n: int, binning: str = "exact"):
+    """The benchmark's frame, device resident, n times on the default stream
+    (with the committed capacity model when binning is "predicted")."""
     import torch
     import gbr
 
@@ -501,8 +563,13 @@ def profile_frames(n: int):
     r = gbr.Renderer(WIDTH, HEIGHT)
     r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, CHUNK)
     r.bind_mesh_device(d_vert.data_ptr(), len(mesh.vertices), mesh.vertex_format)
-    for _ in range(n):
+    if binning == "predicted":
+        import predictor
+        predictor.install(r)
+    for i in range(n):
         r.render_scene(scene)
+        if i == 0:
+            r.stats()   # the first frame sizes the bin storage (predicted capacities)
     st = r.stats()
     torch.cuda.synchronize(dev)
     r.close()
@@ -519,6 +586,8 @@ def main():
     ap.add_argument("--workload", choices=["soup", "batch", "icosphere"], default="soup",
                     help="soup: the 1M-triangle 1080p frame; batch: 256 uneven soups as one batched frame; "
                          "icosphere: the lit 4K icosphere with 8x8 and 16x16 bins")
+    ap.add_argument("--binning", choices=["exact", "predicted"], default="exact",
+                    help="binning of the --profile-frames frames")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="render this many device-resident frames and exit (for a profiler)")
     args = ap.parse_args()
@@ -526,7 +595,7 @@ def main():
     if args.profile_frames:
         import build as gbr_build
         gbr_build.build()
-        profile_frames(args.profile_frames)
+        profile_frames(args.profile_frames, args.binning)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

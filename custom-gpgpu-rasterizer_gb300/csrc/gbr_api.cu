@@ -133,8 +133,8 @@ uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_
 
 void free_bins(gbr_renderer* r) {
     cudaFree(r->d_counts); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
-    cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_partial);
-    r->d_partial = nullptr;
+    cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_scan);
+    r->d_scan = nullptr;
     cudaFree(r->d_feat); cudaFree(r->d_features_out);
     r->d_feat = nullptr;
     r->d_features_out = nullptr;
@@ -251,7 +251,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.items = r->d_items; F.items_cap = r->items_cap;
     F.list = r->d_list; F.list_cap = r->list_cap;
     F.ctl = r->d_ctl;
-    F.scan_partial = r->d_partial;
+    F.scan_state = r->d_scan;
     const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
     F.feat = r->d_feat;
     F.mlp_w = r->d_mlp_w;
@@ -260,6 +260,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.sample_stride = kSampleStride;
     F.exact_guard = predicted ? 1u : 0u;
 
+    const bool stages = r->timing == GBR_TIMING_STAGES;
     if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[0], s));
     GBR_CUDA(cudaMemsetAsync(r->d_ctl, 0, sizeof(Ctl), s));
     if (predicted) {
@@ -269,7 +270,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         GBR_CUDA(launch_capacity(F, true, s));
         GBR_CUDA(launch_scan(scan_of(F, kScanCapacity), s));
         GBR_CUDA(launch_setup(F, true, s));
-        if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
+        if (stages) GBR_CUDA(cudaEventRecord(r->ev[1], s));
         GBR_CUDA(launch_scan(scan_of(F, kScanPredictedItems), s));
         GBR_CUDA(launch_setup(F, false, s));
         GBR_CUDA(launch_scan(scan_of(F, kScanExactAfterPredicted), s));
@@ -281,13 +282,15 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
             GBR_CUDA(launch_feat_reset(F, s));
         }
         GBR_CUDA(launch_setup(F, false, s));
-        if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[1], s));
+        if (stages) GBR_CUDA(cudaEventRecord(r->ev[1], s));
         GBR_CUDA(launch_scan(scan_of(F, kScanExact), s));
         GBR_CUDA(launch_fill(F, s));
     }
     r->last_predicted = predicted;
-    if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[2], s));
+    if (stages) GBR_CUDA(cudaEventRecord(r->ev[2], s));
     GBR_CUDA(launch_raster(F, (uint32_t)(r->num_sms * r->raster_blocks_per_sm), s));
+    if (stages) GBR_CUDA(cudaEventRecord(r->ev[4], s));
+    GBR_CUDA(launch_shade(F, s));
     if (r->timing) {
         GBR_CUDA(cudaEventRecord(r->ev[3], s));
         r->ev_recorded = true;
@@ -314,6 +317,10 @@ gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
         GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     }
     if (r->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "bin storage overflow persists");
+    if (r->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
+        GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(r->nbx * r->nby)));
+        return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the frame is invalid");
+    }
     // predicted capacities that did not fit the list: grow it for the next
     // frames, within reason (the frame itself was re-binned exactly)
     const uint64_t want = r->h_ctl->pred_capacity;
@@ -405,7 +412,8 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     GBR_CUDA(cudaMalloc(&r->d_capacity, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_capacity, 0, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_bin_done, nb * sizeof(uint32_t)));
-    GBR_CUDA(cudaMalloc(&r->d_partial, 2u * scan_blocks(nb) * sizeof(unsigned long long)));
+    GBR_CUDA(cudaMalloc(&r->d_scan, scan_state_bytes(nb)));
+    GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(nb)));
     GBR_CUDA(cudaMemset(r->d_bin_done, 0, nb * sizeof(uint32_t)));
     // pre-pass accumulators: slot 4 (depth min) starts at all ones, the rest at 0
     GBR_CUDA(cudaMalloc(&r->d_feat, (size_t)kFeatSlots * nb * sizeof(uint32_t)));
@@ -583,9 +591,10 @@ gbr_status gbr_set_raster_params(gbr_renderer* r, uint32_t phase, uint32_t ctas_
     return GBR_OK;
 }
 
-gbr_status gbr_set_timing(gbr_renderer* r, int enabled) {
+gbr_status gbr_set_timing(gbr_renderer* r, int mode) {
     if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
-    r->timing = enabled != 0;
+    if (mode < GBR_TIMING_OFF || mode > GBR_TIMING_TOTAL) return fail(GBR_ERR_INVALID_ARG, "unknown timing mode");
+    r->timing = mode;
     return GBR_OK;
 }
 
@@ -739,10 +748,14 @@ gbr_status gbr_get_stats(gbr_renderer* r, gbr_stats* out, void* stream) {
     out->num_float_path = r->h_ctl->num_float_path;
     out->predicted_overflow = r->h_ctl->pred_overflow;
     out->predicted_capacity = r->h_ctl->pred_capacity;
-    if (r->timing && r->ev_recorded) {
+    out->ms_setup = out->ms_bin = out->ms_raster = out->ms_shade = out->ms_total = 0.f;
+    if (r->timing == GBR_TIMING_TOTAL && r->ev_recorded) {
+        cudaEventElapsedTime(&out->ms_total, r->ev[0], r->ev[3]);
+    } else if (r->timing && r->ev_recorded) {
         cudaEventElapsedTime(&out->ms_setup, r->ev[0], r->ev[1]);
         cudaEventElapsedTime(&out->ms_bin, r->ev[1], r->ev[2]);
-        cudaEventElapsedTime(&out->ms_raster, r->ev[2], r->ev[3]);
+        cudaEventElapsedTime(&out->ms_raster, r->ev[2], r->ev[4]);
+        cudaEventElapsedTime(&out->ms_shade, r->ev[4], r->ev[3]);
         cudaEventElapsedTime(&out->ms_total, r->ev[0], r->ev[3]);
     }
     return GBR_OK;

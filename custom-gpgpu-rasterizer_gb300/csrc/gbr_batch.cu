@@ -68,7 +68,7 @@ struct gbr_batch {
     uint32_t* d_counts = nullptr;
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
-    unsigned long long* d_partial = nullptr;   // bin scan scratch
+    ScanState* d_scan = nullptr;   // bin scan state (zeroed once)
     TriSetup* d_setup = nullptr;
     uint2* d_rects = nullptr;
     uint32_t* d_list = nullptr;
@@ -108,9 +108,9 @@ void drop_graph(gbr_batch* b) {
 
 void free_layout_storage(gbr_batch* b) {
     cudaFree(b->d_tables); cudaFree(b->d_counts); cudaFree(b->d_offsets); cudaFree(b->d_cursors);
-    cudaFree(b->d_setup); cudaFree(b->d_rects); cudaFree(b->d_partial);
+    cudaFree(b->d_setup); cudaFree(b->d_rects); cudaFree(b->d_scan);
     b->d_tables = b->d_counts = b->d_offsets = b->d_cursors = nullptr;
-    b->d_partial = nullptr;
+    b->d_scan = nullptr;
     b->d_setup = nullptr;
     b->d_rects = nullptr;
 }
@@ -200,7 +200,8 @@ gbr_status ensure_layout(gbr_batch* b) {
     // one scan over the bins of every scene: scene s's offsets are entries
     // [bin_base[s], bin_base[s+1]] of the batch-wide array
     GBR_CUDA(cudaMalloc(&b->d_offsets, (bins + 1u) * sizeof(uint32_t)));
-    GBR_CUDA(cudaMalloc(&b->d_partial, 2u * scan_blocks((uint32_t)bins) * sizeof(unsigned long long)));
+    GBR_CUDA(cudaMalloc(&b->d_scan, scan_state_bytes((uint32_t)bins)));
+    GBR_CUDA(cudaMemset(b->d_scan, 0, scan_state_bytes((uint32_t)bins)));
     GBR_CUDA(cudaMalloc(&b->d_cursors, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&b->d_setup, std::max<uint64_t>(tris, 1u) * sizeof(TriSetup)));
     GBR_CUDA(cudaMalloc(&b->d_rects, std::max<uint64_t>(tris, 1u) * sizeof(uint2)));
@@ -293,7 +294,7 @@ gbr_status capture_graph(gbr_batch* b) {
     L.scan.offsets = b->d_offsets;
     L.scan.cursors = b->d_cursors;
     L.scan.items = b->d_items;
-    L.scan.partial = b->d_partial;
+    L.scan.state = b->d_scan;
     L.scan.ctl = b->d_ctl;
     L.scan.list_cap = b->list_cap;
     L.scan.items_cap = b->items_cap;
@@ -363,6 +364,10 @@ gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
         GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     }
     if (b->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "batch bin storage overflow persists");
+    if (b->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
+        GBR_CUDA(cudaMemset(b->d_scan, 0, scan_state_bytes(b->total_bins)));
+        return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the batch frame is invalid");
+    }
     return GBR_OK;
 }
 

@@ -128,7 +128,7 @@ struct FrameDev {
     const LightDev* lights;    // scene lights (num_lights == 0: the reference shader's constant light)
     uint32_t num_lights;
     uint32_t flat_shade;      // PBR view and no mesh with a diffuse map: pixels shade from vertex colours
-    unsigned long long* scan_partial;   // bin scan scratch: 2 per block of 1024 bins
+    struct ScanState* scan_state;   // bin scan scratch (scan_state_bytes)
     uint32_t pad_scan[2];
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
@@ -140,13 +140,36 @@ enum : uint32_t {
     kScanExactAfterPredicted = 2,  // as kScanExact, run only after a predicted overflow
     kScanPredictedItems = 3        // filled sizes within the capacities -> work items
 };
+// Single-pass bin scan (decoupled look-back): tiles of 1024 bins take
+// tickets in launch order, publish their totals, then their inclusive
+// prefixes; a tile sums its predecessors' totals back to the nearest
+// published prefix.  Flags carry the scan's sequence tag, so the state needs
+// zeroing once when allocated and never between scans.
+struct ScanTile {
+    uint32_t flag;                  // tag << 2 | kTileAggregate / kTilePrefix
+    uint32_t pad;
+    unsigned long long agg_a, agg_b;   // the tile's bin entries and work items
+    unsigned long long inc_a, inc_b;   // inclusive prefixes (valid with kTilePrefix)
+    unsigned long long pad2;
+};
+struct ScanState {
+    uint32_t ticket;                // next tile of the running scan
+    uint32_t seq;                   // scans completed (tags the flags)
+    uint32_t pad[6];
+};
+static_assert(sizeof(ScanTile) == 48 && sizeof(ScanState) == 32, "scan state layout");
+enum : uint32_t { kTileAggregate = 1, kTilePrefix = 2 };
+__host__ __device__ constexpr size_t scan_state_bytes(uint32_t num_bins) {
+    return sizeof(ScanState) + sizeof(ScanTile) * (size_t)(num_bins == 0 ? 1u : (num_bins + 1023u) / 1024u);
+}
+
 struct ScanDev {
     uint32_t* counts;              // exact counts, zeroed for the next frame
     const uint32_t* capacity;      // predicted capacities
     uint32_t* offsets;             // n + 1
     uint32_t* cursors;
     uint4* items;
-    unsigned long long* partial;   // 2 per block of 1024 bins
+    ScanState* state;
     Ctl* ctl;
     uint32_t* feat;                // kScanPredictedItems: pre-pass accumulators to reset (or null)
     unsigned long long list_cap;
@@ -377,26 +400,39 @@ __device__ __forceinline__ bool weights_float(const TriSetup& t, float px, float
     return true;
 }
 
-// Walks the bins of the warp's packed rectangles; called by whole warps.
-// The warp's (triangle, bin) pairs are expanded load-balanced: pair k of the
-// warp belongs to the lane whose exclusive pair prefix is the largest one
-// <= k, so every iteration gives each lane its own pair whatever the spread
-// of rectangle sizes.
+// Position of the n-th lowest set bit of m (1 <= n <= popc(m)).
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t s = 16; s >= 1; s >>= 1) {
+        const uint32_t c = __popc(m & ((1u << s) - 1u));
+        if (c < n) { n -= c; m >>= s; pos += s; }
+    }
+    return pos;
+}
+
+// Walks the bins of the warp's packed rectangles; called by whole warps of
+// 256-thread blocks.  The warp's (triangle, bin) pairs are expanded
+// load-balanced, 32 consecutive pairs per round: the lane whose pair range
+// covers the round's first pair is found with a ballot, the starts of the
+// other ranges inside the round with one OR-reduction, and a lane's pair
+// belongs to the r-th non-empty range after the first, r = the starts at or
+// before it -- integer-pipe work, with one shared-memory load for the
+// owner's rectangle.  A lane takes up to kPairsPerLane pairs per pass and
+// issues their atomics back to back: the fill pass is bound by the latency
+// of its atomics with return, so several must be in flight per lane.
 // Mode 0: count (atomicAdd on counts), 1: fill (append entry), 2: predicted
 // fill (append within the bin's predicted capacity), 3: pre-pass count
-// (atomicAdd on the first feature slot).  GBR_BIN_AGGREGATE 0 (the
-// default) issues one atomic per pair; 1 groups the lanes of a warp that hit
-// the same bin with __match_any_sync and lets one lane do the group's
-// atomic.  On GB300 the grouped form measured ~10% slower on both the 1M
-// soup and the 4K icosphere (the MATCH instruction and the divergent leader
-// branch load the ADU pipe, 88% busy in the fill kernel, while same-bin
-// lanes are rare), so it is built only on request.
-#ifndef GBR_BIN_AGGREGATE
-#define GBR_BIN_AGGREGATE 0
-#endif
+// (atomicAdd on the first feature slot).  One atomic per pair: grouping the
+// lanes of a warp that hit the same bin (__match_any_sync, one atomic per
+// group) measured ~10% slower on GB300 for both the 1M soup and the 4K
+// icosphere, since same-bin lanes are rare and MATCH is costly.
+constexpr uint32_t kPairsPerLane = 4;
+
 template <int MODE>
 __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid) {
-    const uint32_t lane = threadIdx.x & 31u;
+    __shared__ uint4 s_tab[8][32];   // per warp: (first pair, width, bx0 | by0 << 16, entry) of each lane
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bx0 = rect.x & 0xFFFFu, bx1 = rect.x >> 16;
     const uint32_t by0 = rect.y & 0xFFFFu, by1 = (rect.y >> 16) & 0x7FFFu;
     uint32_t w = 0, n = 0;
@@ -411,60 +447,56 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
         if (lane >= d) incl += t;
     }
     const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (total == 0u) return;   // warp-uniform
     const uint32_t excl = incl - n;
-    for (uint32_t base = 0; base < total; base += 32u) {   // warp-uniform
-        const uint32_t k = base + lane;
-        uint32_t o = 0;   // largest lane with excl <= k: the owner of pair k
+    s_tab[warp][lane] = make_uint4(excl, w, bx0 | (by0 << 16), entry);
+    __syncwarp();
+    const uint32_t nonempty = __ballot_sync(0xFFFFFFFFu, n != 0u);
+    const uint32_t upto = lane == 31u ? 0xFFFFFFFFu : ((2u << lane) - 1u);   // bits 0..lane
+    for (uint32_t base = 0; base < total; base += 32u * kPairsPerLane) {   // warp-uniform
+        uint32_t bin[kPairsPerLane], ent[kPairsPerLane];
+        bool act[kPairsPerLane];
 #pragma unroll
-        for (uint32_t step = 16; step >= 1; step >>= 1) {
-            const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, o + step);
-            if (e <= k) o += step;
+        for (uint32_t u = 0; u < kPairsPerLane; ++u) {
+            act[u] = false;
+            bin[u] = 0u;
+            ent[u] = 0u;
+            const uint32_t b = base + u * 32u;
+            if (b >= total) continue;   // warp-uniform
+            const uint32_t start = (n != 0u && excl > b && excl - b < 32u) ? (1u << (excl - b)) : 0u;
+            const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, start);
+            const uint32_t first = (uint32_t)(__ffs(__ballot_sync(0xFFFFFFFFu, n != 0u && excl <= b && b < incl)) - 1);
+            const uint32_t r = (uint32_t)__popc(starts & upto);
+            const uint32_t after = first == 31u ? 0u : nonempty & ~((2u << first) - 1u);
+            const uint32_t o = r == 0u ? first : nth_set_bit(after, r);
+            const uint4 d = s_tab[warp][o & 31u];
+            const uint32_t k = b + lane;
+            act[u] = k < total;
+            const uint32_t j = k - d.x;
+            const uint32_t q = act[u] ? j / d.y : 0u;
+            bin[u] = ((d.z & 0xFFFFu) + (j - q * d.y)) + ((d.z >> 16) + q) * F.nbx;
+            ent[u] = d.w;
         }
-        const uint32_t j = k - __shfl_sync(0xFFFFFFFFu, excl, o);
-        const uint32_t ow = __shfl_sync(0xFFFFFFFFu, w, o);
-        const uint32_t obx = __shfl_sync(0xFFFFFFFFu, bx0, o);
-        const uint32_t oby = __shfl_sync(0xFFFFFFFFu, by0, o);
-        const uint32_t oentry = __shfl_sync(0xFFFFFFFFu, entry, o);
-        const bool act = k < total;
-        const uint32_t q = act ? j / ow : 0u;
-        const uint32_t bin = act ? (obx + (j - q * ow)) + (oby + q) * F.nbx : 0xFFFFFFFFu;
-#if GBR_BIN_AGGREGATE == 0
-        // one atomic per pair, no grouping
-        if (!act) continue;
-        if (MODE == 0) {
-            atomicAdd(&F.counts[bin], 1u);
-        } else if (MODE == 3) {
-            atomicAdd(&F.feat[bin], 1u);
+        if (MODE == 0 || MODE == 3) {
+            uint32_t* const tgt = MODE == 0 ? F.counts : F.feat;
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u)
+                if (act[u]) atomicAdd(&tgt[bin[u]], 1u);
         } else {
-            const uint32_t pos = atomicAdd(&F.cursors[bin], 1u);
-            if (MODE == 1) F.list[pos] = oentry;
-            else if (pos < __ldg(&F.offsets[bin]) + __ldg(&F.capacity[bin])) F.list[pos] = oentry;
-            else atomicOr(&F.ctl->pred_overflow, 1u);
-        }
-        continue;
-#endif
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, bin);
-        if (!act) continue;
-        const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
-        const uint32_t cnt = (uint32_t)__popc(peers);
-        if (MODE == 0) {
-            if (lane == leader) atomicAdd(&F.counts[bin], cnt);
-        } else if (MODE == 3) {
-            if (lane == leader) atomicAdd(&F.feat[bin], cnt);
-        } else {
-            uint32_t pos0 = 0;
-            if (lane == leader) pos0 = atomicAdd(&F.cursors[bin], cnt);
-            pos0 = __shfl_sync(peers, pos0, (int)leader);
-            const uint32_t pos = pos0 + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-            if (MODE == 1) {
-                F.list[pos] = oentry;
-            } else {
+            uint32_t pos[kPairsPerLane];
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) pos[u] = act[u] ? atomicAdd(&F.cursors[bin[u]], 1u) : 0u;
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) {
+                if (!act[u]) continue;
+                if (MODE == 1) F.list[pos[u]] = ent[u];
                 // cursors start at the bin's offset; the bin owns capacity[bin] slots
-                if (pos < __ldg(&F.offsets[bin]) + __ldg(&F.capacity[bin])) F.list[pos] = oentry;
-                else if (lane == leader) atomicOr(&F.ctl->pred_overflow, 1u);
+                else if (pos[u] < __ldg(&F.offsets[bin[u]]) + __ldg(&F.capacity[bin[u]])) F.list[pos[u]] = ent[u];
+                else atomicOr(&F.ctl->pred_overflow, 1u);
             }
         }
     }
+    __syncwarp();   // the warp's table row is rewritten by its next walk
 }
 
 }  // namespace gbr

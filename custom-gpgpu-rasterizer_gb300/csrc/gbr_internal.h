@@ -51,7 +51,7 @@ struct gbr_renderer {
     uint32_t nbx = 0, nby = 0, bw = 0, bh = 0, chunk = 256;
     bool bins_ready = false;
     uint32_t binning = GBR_BINNING_EXACT;
-    bool timing = false;
+    int timing = 0;           // GBR_TIMING_*
     int raster_blocks_per_sm = 1;
     uint32_t raster_phase = 0;   // 0: library default
     uint32_t raster_ctas = 0;    // 0: library default
@@ -78,7 +78,7 @@ struct gbr_renderer {
     uint32_t* d_cursors = nullptr;
     uint32_t* d_capacity = nullptr;
     uint32_t* d_bin_done = nullptr;
-    unsigned long long* d_partial = nullptr;   // bin scan scratch
+    gbr::ScanState* d_scan = nullptr;   // bin scan state (zeroed once)
     uint4* d_items = nullptr;
     uint32_t items_cap = 0;
     uint32_t* d_list = nullptr;

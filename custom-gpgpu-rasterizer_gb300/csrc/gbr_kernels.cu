@@ -16,6 +16,7 @@
 // Reference stages replaced: VS_Kernel, TA_Kernel, TB_Kernel,
 // RA_PerTileKernel, PS_Kernel and the CLEAR_* kernels
 // (CustomCUDARasterizer/CUDARenderer.cu:598-1129, launchers :1625-1966).
+#include <algorithm>
 #include <cstring>
 
 #include "gbr_device.cuh"
@@ -119,10 +120,15 @@ __device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim) {
 
 template <int MODE>
 __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
+    pdl_wait();
     // predicted binning: the exact pass only runs after an overflow, and the
     // predicted pass stops once an overflow is known
     if (MODE == 0 ? (F.exact_guard && !F.ctl->pred_overflow) : (F.ctl->pred_overflow != 0u)) return;
-    setup_tri<MODE>(F, blockIdx.x * blockDim.x + threadIdx.x);
+    // a resident grid strides over the triangles, so that a guarded launch
+    // that does not run costs one wave of early exits
+    for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x)
+        setup_tri<MODE>(F, base + threadIdx.x);
+    pdl_release();
 }
 
 // Second pass of exact binning for triangle `prim`.  Called by whole warps.
@@ -134,8 +140,11 @@ __device__ __forceinline__ void fill_tri(const FrameDev& F, uint32_t prim) {
 }
 
 __global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
+    pdl_wait();
     if (F.ctl->overflow || (F.exact_guard && !F.ctl->pred_overflow)) return;
-    fill_tri(F, blockIdx.x * blockDim.x + threadIdx.x);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x)
+        fill_tri(F, base + threadIdx.x);
+    pdl_release();
 }
 
 // ---------------------------------------------------------------------------
@@ -203,16 +212,21 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
     const int dxa = X1 - X0, dya = Y1 - Y0;
     const int dxb = X2 - X1, dyb = Y2 - Y1;
     const int dxc = X0 - X2, dyc = Y0 - Y2;
-    for (int sy = py0; sy <= py1; sy += sh) {
+    // exact edge values at the lane's first pixel, then stepped by whole
+    // stamps: E(x + sw, y) = E + sw * 2^16 * dy, E(x, y + sh) = E - sh * 2^16 * dx
+    const int fx0 = (px0 + lx) << kFxBits, fy0 = (py0 + ly) << kFxBits;
+    long long r2 = edge_fx(fx0, fy0, X0, Y0, dxa, dya);
+    long long r0 = edge_fx(fx0, fy0, X1, Y1, dxb, dyb);
+    long long r1 = edge_fx(fx0, fy0, X2, Y2, dxc, dyc);
+    const long long stx = (long long)sw << kFxBits, sty = (long long)sh << kFxBits;
+    const long long ix2 = stx * dya, ix0 = stx * dyb, ix1 = stx * dyc;
+    const long long iy2 = -sty * dxa, iy0 = -sty * dxb, iy1 = -sty * dxc;
+    for (int sy = py0; sy <= py1; sy += sh, r2 += iy2, r0 += iy0, r1 += iy1) {
         const int y = sy + ly;
-        for (int sx = px0; sx <= px1; sx += sw) {
+        long long e2 = r2, e0 = r0, e1 = r1;
+        for (int sx = px0; sx <= px1; sx += sw, e2 += ix2, e0 += ix0, e1 += ix1) {
             const int x = sx + lx;
-            if (x > px1 || y > py1) continue;
-            const int Px = x << kFxBits, Py = y << kFxBits;
-            const long long e2 = edge_fx(Px, Py, X0, Y0, dxa, dya);
-            const long long e0 = edge_fx(Px, Py, X1, Y1, dxb, dyb);
-            const long long e1 = edge_fx(Px, Py, X2, Y2, dxc, dyc);
-            if ((e0 | e1 | e2) < 0) continue;
+            if (x > px1 || y > py1 || (e0 | e1 | e2) < 0) continue;
             float w[3];
             weights_fixed(t, x, y, w);
             const float z = interp_z(w[0], w[1], w[2], t.z0, t.z1, t.z2);
@@ -291,6 +305,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RasterShared& S = *reinterpret_cast<RasterShared*>(smem_raw);
     unsigned long long* tile = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(RasterShared));
+    pdl_wait();
     Ctl* const Q = BATCH ? B.ctl : F.ctl;
     const uint4* const items = BATCH ? B.items : F.items;
     if (Q->overflow) return;
@@ -444,6 +459,7 @@ __device__ __forceinline__ void shade_px(const FrameDev& F, uint32_t i) {
 // One thread per pixel.
 template <bool FLAT>
 __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
+    pdl_wait();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.width * F.height || F.ctl->overflow) return;
     shade_px<FLAT>(F, i);
@@ -528,43 +544,51 @@ size_t raster_smem_bytes(uint32_t bw, uint32_t bh) {
     return sizeof(RasterShared) + (size_t)bw * bh * sizeof(unsigned long long);
 }
 
+// Blocks of 256 threads for a triangle pass: one per 256 triangles, at most
+// one resident wave (8 per SM).
+static uint32_t triangle_blocks(uint32_t num_tris) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 152;
+    return std::min<uint32_t>((num_tris + 255u) / 256u, 8u * (uint32_t)sms);
+}
+
 cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s) {
-    const uint32_t blocks = (F.num_tris + 255u) / 256u;
+    const uint32_t blocks = triangle_blocks(F.num_tris);
     if (blocks == 0) return cudaSuccess;
-    if (predicted) setup_kernel<1><<<blocks, 256, 0, s>>>(F);
-    else setup_kernel<0><<<blocks, 256, 0, s>>>(F);
-    return cudaGetLastError();
+    return predicted ? launch_pdl(setup_kernel<1>, dim3(blocks), dim3(256), 0, s, F)
+                     : launch_pdl(setup_kernel<0>, dim3(blocks), dim3(256), 0, s, F);
 }
 
 cudaError_t launch_fill(const FrameDev& F, cudaStream_t s) {
-    const uint32_t blocks = (F.num_tris + 255u) / 256u;
+    const uint32_t blocks = triangle_blocks(F.num_tris);
     if (blocks == 0) return cudaSuccess;
-    fill_kernel<<<blocks, 256, 0, s>>>(F);
-    return cudaGetLastError();
+    return launch_pdl(fill_kernel, dim3(blocks), dim3(256), 0, s, F);
 }
 
 template <bool BATCH>
 static cudaError_t launch_raster_variant(const FrameDev& F, const BatchDev& B, uint32_t ctas, uint32_t grid, size_t smem,
                                          cudaStream_t s) {
+    const dim3 g(grid), b(kRasterThreads);
     switch (ctas ? ctas : kDefaultRasterCtas) {
-        case 2: raster_kernel<2, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
-        case 3: raster_kernel<3, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
-        case 5: raster_kernel<5, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
-        case 6: raster_kernel<6, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
-        default: raster_kernel<4, BATCH><<<grid, kRasterThreads, smem, s>>>(F, B); break;
+        case 2: return launch_pdl(raster_kernel<2, BATCH>, g, b, smem, s, F, B);
+        case 3: return launch_pdl(raster_kernel<3, BATCH>, g, b, smem, s, F, B);
+        case 5: return launch_pdl(raster_kernel<5, BATCH>, g, b, smem, s, F, B);
+        case 6: return launch_pdl(raster_kernel<6, BATCH>, g, b, smem, s, F, B);
+        default: return launch_pdl(raster_kernel<4, BATCH>, g, b, smem, s, F, B);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
     BatchDev none;
     memset(&none, 0, sizeof none);
-    cudaError_t e = launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
-    if (e != cudaSuccess) return e;
+    return launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
+}
+
+cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
     const uint32_t npx = F.width * F.height;
-    if (F.flat_shade) shade_kernel<true><<<(npx + 255u) / 256u, 256, 0, s>>>(F);
-    else shade_kernel<false><<<(npx + 255u) / 256u, 256, 0, s>>>(F);
-    return cudaGetLastError();
+    const dim3 g((npx + 255u) / 256u), b(256);
+    return F.flat_shade ? launch_pdl(shade_kernel<true>, g, b, 0, s, F) : launch_pdl(shade_kernel<false>, g, b, 0, s, F);
 }
 
 cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s) {

@@ -6,17 +6,42 @@
 
 namespace gbr {
 
+// Programmatic dependent launch (sm_90+): a kernel started with launch_pdl
+// may be scheduled while the kernel before it in the stream is finishing;
+// it calls pdl_wait() before it touches anything, which returns once that
+// kernel has completed and its writes are visible.  A kernel calls
+// pdl_release() when its own work is issued, letting the next one launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 size_t raster_smem_bytes(uint32_t bw, uint32_t bh);
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm);
 // ctas: the raster_kernel variant compiled for 2..6 CTAs per SM (0: default)
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
 cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s);
-// The bin scan of a frame (mode: kScanExact, ...) and its three launches.
+// The bin scan of a frame (mode: kScanExact, ...), one launch.
 ScanDev scan_of(const FrameDev& F, uint32_t mode);
-uint32_t scan_blocks(uint32_t num_bins);   // blocks of 1024 bins; FrameDev::scan_partial holds 2 per block
+uint32_t scan_blocks(uint32_t num_bins);   // tiles of 1024 bins
 cudaError_t launch_scan(const ScanDev& S, cudaStream_t s);
 cudaError_t launch_fill(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s);
+cudaError_t launch_shade(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_clear(const FrameDev& F, cudaStream_t s);
 
 // Grid sizes of a batch frame (see BatchDev).

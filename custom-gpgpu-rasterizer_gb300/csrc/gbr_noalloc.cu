@@ -57,8 +57,8 @@ constexpr size_t kOffGvis = kOffList + align256(size_t(kNaMaxPairs) * 4u);
 constexpr size_t kOffIds = kOffGvis + align256(size_t(kNaMaxPixels) * 8u);
 constexpr size_t kOffCtl = kOffIds + align256(size_t(kNaMaxPixels) * 4u);
 constexpr size_t kOffMesh = kOffCtl + align256(sizeof(Ctl));
-constexpr size_t kOffPartial = kOffMesh + align256(sizeof(MeshDev));
-constexpr size_t kScratchBytes = kOffPartial + align256(size_t(2u * (kNaMaxBins / 1024u + 1u)) * 8u);
+constexpr size_t kOffScan = kOffMesh + align256(sizeof(MeshDev));
+constexpr size_t kScratchBytes = kOffScan + align256(scan_state_bytes(kNaMaxBins));
 
 // The only device memory this entry point uses besides the caller's.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -84,6 +84,10 @@ __global__ void noalloc_prepare_kernel(FrameDev F, MeshDev desc, uint32_t npx) {
         F.counts[i] = 0u;
         F.bin_done[i] = 0u;
     }
+    // the caller's scratch: the bin scan state starts zeroed every frame
+    uint32_t* scan = reinterpret_cast<uint32_t*>(F.scan_state);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < scan_state_bytes(F.num_bins) / 4u; i += stride)
+        scan[i] = 0u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *const_cast<MeshDev*>(F.meshes) = desc;
         memset(F.ctl, 0, sizeof(Ctl));
@@ -178,7 +182,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.gvis = reinterpret_cast<unsigned long long*>(b + kOffGvis);
     F.ids = reinterpret_cast<uint32_t*>(b + kOffIds);
     F.ctl = reinterpret_cast<Ctl*>(b + kOffCtl);
-    F.scan_partial = reinterpret_cast<unsigned long long*>(b + kOffPartial);
+    F.scan_state = reinterpret_cast<ScanState*>(b + kOffScan);
     F.colour = d_colour;
     F.depth = d_depth;
 
@@ -204,6 +208,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     if (e == cudaSuccess) e = launch_scan(scan_of(F, kScanExact), s);
     if (e == cudaSuccess) e = launch_fill(F, s);
     if (e == cudaSuccess) e = launch_raster(F, (uint32_t)(slot.num_sms * (blocks_per_sm > 0 ? blocks_per_sm : 1)), s);
+    if (e == cudaSuccess) e = launch_shade(F, s);
     if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
     // the frame is only valid if its bin entries fitted the static storage
     e = cudaStreamSynchronize(s);
@@ -212,5 +217,6 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     e = cudaMemcpy(&ctl, b + kOffCtl, sizeof ctl, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
     if (ctl.overflow) return na_fail(GBR_ERR_OUT_OF_MEMORY, "frame needs more than 2^20 bin entries");
+    if (ctl.error) return na_fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the frame is invalid");
     return GBR_OK;
 }

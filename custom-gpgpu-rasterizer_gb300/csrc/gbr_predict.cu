@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(256) prepass_kernel(FrameDev F) {
     // triangles: a fixed stride would alias with structured index orders
     // (a subdivided mesh numbers its children level by level, so every 8th
     // triangle falls on a few of the base faces only)
+    pdl_wait();
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t first = idx * F.sample_stride;
     uint32_t prim = first + hash32(idx) % F.sample_stride;
@@ -203,40 +204,50 @@ __device__ __forceinline__ void bin_features(const FrameDev& F, uint32_t b, floa
 }
 
 // One warp per bin: lane j holds hidden units j and j + 32 of both layers;
-// layer-2 inputs come from a per-warp copy of h1 in shared memory and the
-// output is a warp reduction.  Every lane returns the pre-softplus output.
-__device__ __forceinline__ float mlp_forward_warp(const float* w, const float* x, float* h1s) {
-    const uint32_t lane = threadIdx.x & 31u;
-    float a = w[kOffB1 + lane], c = w[kOffB1 + lane + 32];
+// the parameters stay BF16 in shared memory (widened to FP32 on use, FP32
+// accumulation), layer-2 inputs come from a per-warp copy of h1 in shared
+// memory, the output is a warp reduction.  Every lane returns the
+// pre-softplus output.
+__device__ __forceinline__ float wbf(const uint16_t* w, int i) { return __uint_as_float((uint32_t)w[i] << 16); }
+
+__device__ __forceinline__ float mlp_forward_warp(const uint16_t* w, const float* x, float* h1s) {
+    const int lane = (int)(threadIdx.x & 31u);
+    float a = wbf(w, kOffB1 + lane), c = wbf(w, kOffB1 + lane + 32);
 #pragma unroll
     for (int k = 0; k < kFeatures; ++k) {
-        a = __fmaf_rn(x[k], w[kOffW1 + k * kMlpHidden + lane], a);
-        c = __fmaf_rn(x[k], w[kOffW1 + k * kMlpHidden + lane + 32], c);
+        a = __fmaf_rn(x[k], wbf(w, kOffW1 + k * kMlpHidden + lane), a);
+        c = __fmaf_rn(x[k], wbf(w, kOffW1 + k * kMlpHidden + lane + 32), c);
     }
     h1s[lane] = fmaxf(a, 0.f);
     h1s[lane + 32] = fmaxf(c, 0.f);
     __syncwarp();
-    float p = w[kOffB2 + lane], q = w[kOffB2 + lane + 32];
+    float p = wbf(w, kOffB2 + lane), q = wbf(w, kOffB2 + lane + 32);
 #pragma unroll 16
     for (int i = 0; i < kMlpHidden; ++i) {
         const float h = h1s[i];
-        p = __fmaf_rn(h, w[kOffW2 + i * kMlpHidden + lane], p);
-        q = __fmaf_rn(h, w[kOffW2 + i * kMlpHidden + lane + 32], q);
+        p = __fmaf_rn(h, wbf(w, kOffW2 + i * kMlpHidden + lane), p);
+        q = __fmaf_rn(h, wbf(w, kOffW2 + i * kMlpHidden + lane + 32), q);
     }
     __syncwarp();   // h1s is reused by the warp's next bin
-    float y = __fmaf_rn(fmaxf(p, 0.f), w[kOffW3 + lane], __fmul_rn(fmaxf(q, 0.f), w[kOffW3 + lane + 32]));
+    float y = __fmaf_rn(fmaxf(p, 0.f), wbf(w, kOffW3 + lane), __fmul_rn(fmaxf(q, 0.f), wbf(w, kOffW3 + lane + 32)));
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) y += __shfl_xor_sync(0xFFFFFFFFu, y, d);
-    return y + w[kOffB3];
+    return y + wbf(w, kOffB3);
 }
 
-// Features of every bin (and, with `predict`, the model's capacity): a
-// persistent grid of warps, one bin per warp at a time, the BF16
-// parameters expanded to FP32 in shared memory once per block.
+// Features of every bin (and, with `predict`, the model's capacity), one
+// bin per warp, the BF16 parameters copied to shared memory once per block
+// with 16-byte loads.
 __global__ void __launch_bounds__(256) capacity_kernel(FrameDev F, int predict) {
-    __shared__ float w[kMlpParams];
+    __shared__ __align__(16) uint16_t w[kMlpParamsPadded];
     __shared__ float h1s[8][kMlpHidden];
-    if (predict) load_params(F.mlp_w, w);
+    pdl_wait();
+    if (predict) {
+        const uint4* src = reinterpret_cast<const uint4*>(F.mlp_w);
+        uint4* dst = reinterpret_cast<uint4*>(w);
+        for (int i = (int)threadIdx.x; i < kMlpParamsPadded / 8; i += (int)blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + warp; b < F.num_bins; b += nwarps) {   // warp-uniform
@@ -387,14 +398,14 @@ __global__ void mlp_adam_kernel(float* master, uint16_t* wq, const float* grad, 
 // ---------------------------------------------------------------------------
 cudaError_t launch_prepass(const FrameDev& F, cudaStream_t s) {
     const uint32_t n = (F.num_tris + F.sample_stride - 1u) / F.sample_stride;
-    if (n) prepass_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(F);
+    if (n) return launch_pdl(prepass_kernel, dim3((n + 255u) / 256u), dim3(256), 0, s, F);
     return cudaGetLastError();
 }
 
 cudaError_t launch_capacity(const FrameDev& F, bool predict, cudaStream_t s) {
-    // 8 warps per block, about four bins per warp, at most 1024 blocks
-    const uint32_t blocks = std::min<uint32_t>((F.num_bins + 31u) / 32u, 1024u);
-    capacity_kernel<<<blocks ? blocks : 1u, 256, 0, s>>>(F, predict ? 1 : 0);
+    // 8 warps per block, one bin per warp up to 4096 blocks (then a few)
+    const uint32_t blocks = std::min<uint32_t>((F.num_bins + 7u) / 8u, 4096u);
+    return launch_pdl(capacity_kernel, dim3(blocks ? blocks : 1u), dim3(256), 0, s, F, predict ? 1 : 0);
     return cudaGetLastError();
 }
 

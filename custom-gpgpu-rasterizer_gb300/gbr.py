@@ -27,6 +27,7 @@ GBR_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "OVERFLOW_RERUN", 4: "TIMEOUT",
                 5: "OUT_OF_MEMORY", 6: "NOT_FOUND"}
 BINNING_EXACT, BINNING_PREDICTED = 0, 1
+TIMING_OFF, TIMING_STAGES, TIMING_TOTAL = 0, 1, 2
 
 EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "gbr_mesh_update_vertices",
             "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
@@ -54,7 +55,8 @@ class Stats(C.Structure):
                 ("num_work_items", C.c_uint64), ("num_float_path", C.c_uint64),
                 ("overflow_reruns", C.c_uint32), ("predicted_overflow", C.c_uint32),
                 ("predicted_capacity", C.c_uint64),
-                ("ms_setup", C.c_float), ("ms_bin", C.c_float), ("ms_raster", C.c_float), ("ms_total", C.c_float)]
+                ("ms_setup", C.c_float), ("ms_bin", C.c_float), ("ms_raster", C.c_float), ("ms_total", C.c_float),
+                ("ms_shade", C.c_float), ("pad", C.c_float)]
 
 
 class Light(C.Structure):
@@ -265,8 +267,12 @@ class Renderer:
     def set_raster_params(self, phase: int = 0, ctas_per_sm: int = 0):
         check(self._lib.gbr_set_raster_params(self.h, phase, ctas_per_sm))
 
-    def set_timing(self, on: bool):
-        check(self._lib.gbr_set_timing(self.h, 1 if on else 0))
+    def set_timing(self, on: bool, total_only: bool = False):
+        """CUDA-event times in stats(): per stage (an event between every
+        stage), or with total_only the frame time alone, which leaves the
+        stages' launches free to overlap."""
+        mode = (TIMING_TOTAL if total_only else TIMING_STAGES) if on else TIMING_OFF
+        check(self._lib.gbr_set_timing(self.h, mode))
 
     # -- frame ---------------------------------------------------------
     def render(self, camera, cull: int, sample: int, vis: int, stream: int = 0):

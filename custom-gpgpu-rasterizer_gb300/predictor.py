@@ -36,6 +36,7 @@ import scenes  # noqa: E402
 
 WEIGHTS = os.path.join(HERE, "predictor_weights.npz")
 NUM_FEATURES = 12
+SAMPLED_SCALE = 256.0   # feature 0 = (8 x sampled pairs of the bin) / 256 (gbr_predict.cu: bin_features)
 
 
 def num_params() -> int:
@@ -274,7 +275,7 @@ def main():
     alpha, beta, gamma = fit_rule(lam, yv)
     cap = capacity(lam, alpha, beta, gamma)
     # the same rule on the plain sampled estimate (8 x sampled pairs) for comparison
-    lam0 = np.expm1(Xv[:, 0])
+    lam0 = Xv[:, 0] * SAMPLED_SCALE
     a0, b0, g0 = fit_rule(lam0, yv)
     cap0 = capacity(lam0, a0, b0, g0)
     meta = {"pairs": int(len(y)), "frames": len(frames), "epochs": args.epochs, "loss": hist,

@@ -76,6 +76,8 @@ typedef struct {
     uint32_t predicted_overflow; /* last predicted-capacity frame overflowed a bin */
     uint64_t predicted_capacity; /* sum of predicted per-bin capacities, last frame */
     float ms_setup, ms_bin, ms_raster, ms_total; /* per-stage times of the last frame with timing on */
+    float ms_shade;              /* the shade pass (included in ms_total, not in ms_raster) */
+    float pad;
 } gbr_stats;
 
 /* CUDARenderer(const WindowHelper&) (CUDARenderer.cu:33-46): headless, the
@@ -173,8 +175,12 @@ gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
  * phase = triangles rasterised between hierarchical-z refreshes (0: 16),
  * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
 gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
-/* Record per-stage CUDA-event times into gbr_stats (off by default). */
-gbr_status gbr_set_timing(gbr_renderer *r, int enabled);
+/* Record CUDA-event times into gbr_stats (off by default).
+ * GBR_TIMING_STAGES records an event between every stage, which also keeps
+ * consecutive kernels from overlapping their launch; GBR_TIMING_TOTAL times
+ * only the whole frame (ms_total; the stage times read 0). */
+enum { GBR_TIMING_OFF = 0, GBR_TIMING_STAGES = 1, GBR_TIMING_TOTAL = 2 };
+gbr_status gbr_set_timing(gbr_renderer *r, int mode);
 
 /* EnterValidRenderingState + Render (CUDARenderer.cu:206-381): clears, runs
  * the whole frame on `stream` and returns without synchronising.  The
