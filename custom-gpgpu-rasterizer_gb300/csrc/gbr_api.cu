@@ -155,7 +155,8 @@ gbr_status ensure_list(gbr_renderer* r, uint64_t pairs) {
     r->d_list = nullptr;
     r->d_items = nullptr;
     const uint64_t items = (uint64_t)nb + cap / r->chunk + 1u;
-    if (cudaMalloc(&r->d_list, cap * sizeof(uint32_t)) != cudaSuccess ||
+    // the bin list, then as many rank slots (exact binning's count pass)
+    if (cudaMalloc(&r->d_list, 2u * cap * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&r->d_items, items * sizeof(uint4)) != cudaSuccess) {
         cudaGetLastError();
         r->list_cap = 0;
@@ -171,11 +172,17 @@ gbr_status ensure_tris(gbr_renderer* r, uint64_t tris) {
     if (tris <= r->tri_cap && r->d_setup) return GBR_OK;
     cudaFree(r->d_setup);
     cudaFree(r->d_rects);
+    cudaFree(r->d_walk);
+    cudaFree(r->d_keys);
     r->d_setup = nullptr;
     r->d_rects = nullptr;
+    r->d_walk = nullptr;
+    r->d_keys = nullptr;
     const uint64_t cap = std::max<uint64_t>(tris, 1024u);
     if (cudaMalloc(&r->d_setup, cap * sizeof(TriSetup)) != cudaSuccess ||
-        cudaMalloc(&r->d_rects, cap * sizeof(uint2)) != cudaSuccess) {
+        cudaMalloc(&r->d_rects, cap * sizeof(uint2)) != cudaSuccess ||
+        cudaMalloc(&r->d_walk, (cap / 32u + 8u) * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&r->d_keys, cap * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
         r->tri_cap = 0;
         return fail(GBR_ERR_OUT_OF_MEMORY, "cannot allocate setup records for %llu triangles", (unsigned long long)tris);
@@ -245,11 +252,13 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.phase = r->raster_phase;
     F.raster_ctas = r->raster_ctas;
     F.meshes = r->d_meshes;
-    F.setup = r->d_setup; F.rects = r->d_rects;
+    F.setup = r->d_setup; F.rects = r->d_rects; F.keys = r->d_keys;
     F.counts = r->d_counts; F.offsets = r->d_offsets; F.cursors = r->d_cursors; F.capacity = r->d_capacity;
     F.bin_done = r->d_bin_done;
     F.items = r->d_items; F.items_cap = r->items_cap;
     F.list = r->d_list; F.list_cap = r->list_cap;
+    F.ranks = r->d_list + r->list_cap; F.rank_cap = r->list_cap;
+    F.walk_base = r->d_walk; F.rank_next = &r->d_ctl->rank_next;
     F.ctl = r->d_ctl;
     F.scan_state = r->d_scan;
     const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
@@ -381,7 +390,7 @@ gbr_status gbr_destroy(gbr_renderer* r) {
     for (TexHost& t : r->textures) cudaFree(t.d_px);
     free_bins(r);
     cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis);
-    cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_meshes); cudaFree(r->d_ctl); cudaFree(r->d_mlp_w);
+    cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_walk); cudaFree(r->d_keys); cudaFree(r->d_meshes); cudaFree(r->d_ctl); cudaFree(r->d_mlp_w);
     cudaFree(r->d_lights);
     cudaFreeHost(r->h_meshes); cudaFreeHost(r->h_ctl);
     if (r->meshes_evt) cudaEventDestroy(r->meshes_evt);
@@ -579,8 +588,8 @@ gbr_status gbr_set_binning(gbr_renderer* r, uint32_t method) {
 }
 
 gbr_status gbr_set_raster_params(gbr_renderer* r, uint32_t phase, uint32_t ctas_per_sm) {
-    if (!r || phase > 4096u || (ctas_per_sm != 0 && (ctas_per_sm < 2 || ctas_per_sm > 6)))
-        return fail(GBR_ERR_INVALID_ARG, "phase %u (0..4096) / ctas_per_sm %u (0, 2..6)", phase, ctas_per_sm);
+    if (!r || phase > kMaxPhase || (ctas_per_sm != 0 && (ctas_per_sm < 2 || ctas_per_sm > 6)))
+        return fail(GBR_ERR_INVALID_ARG, "phase %u (0..%u) / ctas_per_sm %u (0, 2..6)", phase, kMaxPhase, ctas_per_sm);
     r->raster_phase = phase;
     r->raster_ctas = ctas_per_sm;
     if (r->bins_ready) {

@@ -71,6 +71,8 @@ struct gbr_batch {
     ScanState* d_scan = nullptr;   // bin scan state (zeroed once)
     TriSetup* d_setup = nullptr;
     uint2* d_rects = nullptr;
+    uint32_t* d_walk = nullptr;     // first rank slot of each 32-triangle walk (8 per block)
+    uint32_t* d_keys = nullptr;     // per-triangle depth-key bounds
     uint32_t* d_list = nullptr;
     uint64_t list_cap = 0;
     uint4* d_items = nullptr;
@@ -108,11 +110,13 @@ void drop_graph(gbr_batch* b) {
 
 void free_layout_storage(gbr_batch* b) {
     cudaFree(b->d_tables); cudaFree(b->d_counts); cudaFree(b->d_offsets); cudaFree(b->d_cursors);
-    cudaFree(b->d_setup); cudaFree(b->d_rects); cudaFree(b->d_scan);
+    cudaFree(b->d_setup); cudaFree(b->d_rects); cudaFree(b->d_scan); cudaFree(b->d_walk); cudaFree(b->d_keys);
     b->d_tables = b->d_counts = b->d_offsets = b->d_cursors = nullptr;
     b->d_scan = nullptr;
     b->d_setup = nullptr;
     b->d_rects = nullptr;
+    b->d_walk = nullptr;
+    b->d_keys = nullptr;
 }
 
 gbr_status ensure_list(gbr_batch* b, uint64_t pairs, uint64_t items) {
@@ -128,7 +132,8 @@ gbr_status ensure_list(gbr_batch* b, uint64_t pairs, uint64_t items) {
     cudaFree(b->d_items);
     b->d_list = nullptr;
     b->d_items = nullptr;
-    if (cudaMalloc(&b->d_list, cap * sizeof(uint32_t)) != cudaSuccess ||
+    // the bin list, then as many rank slots (exact binning's count pass)
+    if (cudaMalloc(&b->d_list, 2u * cap * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&b->d_items, icap * sizeof(uint4)) != cudaSuccess) {
         cudaGetLastError();
         b->list_cap = 0;
@@ -205,6 +210,8 @@ gbr_status ensure_layout(gbr_batch* b) {
     GBR_CUDA(cudaMalloc(&b->d_cursors, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&b->d_setup, std::max<uint64_t>(tris, 1u) * sizeof(TriSetup)));
     GBR_CUDA(cudaMalloc(&b->d_rects, std::max<uint64_t>(tris, 1u) * sizeof(uint2)));
+    GBR_CUDA(cudaMalloc(&b->d_walk, std::max<uint64_t>(tri_blocks, 1u) * 8u * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&b->d_keys, std::max<uint64_t>(tris, 1u) * sizeof(uint32_t)));
     gbr_status st = ensure_list(b, std::max<uint64_t>(b->list_cap, 4u * tris), b->items_cap);
     if (st != GBR_OK) return st;
 
@@ -253,11 +260,16 @@ void build_table(gbr_batch* b, std::vector<unsigned char>& out) {
         F.meshes = d_meshes + L.mesh_base;
         F.setup = b->d_setup + L.tri_base;
         F.rects = b->d_rects + L.tri_base;
+        F.keys = b->d_keys + L.tri_base;
         F.counts = b->d_counts + L.bin_base;
         F.offsets = b->d_offsets + L.bin_base;
         F.cursors = b->d_cursors + L.bin_base;
         F.list = b->d_list;
         F.list_cap = b->list_cap;
+        F.ranks = b->d_list + b->list_cap;
+        F.rank_cap = b->list_cap;
+        F.walk_base = b->d_walk;          // walks are numbered over the whole batch grid
+        F.rank_next = &b->d_ctl->rank_next;
         F.ctl = m.r->d_ctl;
         memcpy(frames + i, &F, sizeof F);
     }
@@ -378,7 +390,7 @@ gbr_status check_state(uint32_t cull, uint32_t sample, uint32_t vis) {
 }
 
 gbr_status check_config(const gbr_batch_config& c) {
-    if (c.bin_size == 0 || c.bin_size > (uint32_t)kMaxBinDim || c.queue_chunk == 0 || c.raster_phase > 4096u ||
+    if (c.bin_size == 0 || c.bin_size > (uint32_t)kMaxBinDim || c.queue_chunk == 0 || c.raster_phase > kMaxPhase ||
         (c.raster_ctas != 0 && (c.raster_ctas < 2 || c.raster_ctas > 6)))
         return fail(GBR_ERR_INVALID_ARG, "batch config: bin %u (1..%d), chunk %u (>= 1), ctas %u (0, 2..6), phase %u",
                     c.bin_size, kMaxBinDim, c.queue_chunk, c.raster_ctas, c.raster_phase);

@@ -22,8 +22,10 @@ constexpr uint32_t kFlagRaster = 1u;              // fixed path, covered winding
 constexpr uint32_t kFlagFloat = 2u;               // outside the guard band: float edge functions
 constexpr int kMaxBinDim = 64;
 constexpr int kRasterThreads = 256;
-constexpr int kBatch = 256;
+constexpr int kBatch = 2048;                      // bin entries the raster depth-sorts at once
+constexpr int kDepthBuckets = 256;                // front-to-back buckets: top 8 bits of the depth key
 constexpr uint32_t kPhase = 16;                   // triangles between hierarchical-z refreshes
+constexpr uint32_t kMaxPhase = 64;                // setup records staged per phase
 constexpr uint32_t kDefaultRasterCtas = 6;        // raster_kernel variant (CTAs per SM) used by default
 
 enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
@@ -86,7 +88,8 @@ struct Ctl {
     uint32_t error;            // non-zero: a bounded wait gave up
     uint32_t num_sampled;      // visible triangles seen by the coarse pre-pass
     unsigned long long items_alloc;   // batch: work items requested by all scenes
-    uint32_t pad[2];
+    uint32_t rank_next;        // exact binning: rank slots reserved by the count pass
+    uint32_t pad;
 };
 static_assert(sizeof(Ctl) == 64, "control block is 64 bytes");
 
@@ -104,6 +107,7 @@ struct FrameDev {
     const MeshDev* meshes;
     TriSetup* setup;
     uint2* rects;
+    uint32_t* keys;            // per triangle: lower bound of its fragments' depth keys (hiz_key)
     uint32_t* counts;
     uint32_t* offsets;        // num_bins + 1
     uint32_t* cursors;
@@ -129,7 +133,12 @@ struct FrameDev {
     uint32_t num_lights;
     uint32_t flat_shade;      // PBR view and no mesh with a diffuse map: pixels shade from vertex colours
     struct ScanState* scan_state;   // bin scan scratch (scan_state_bytes)
-    uint32_t pad_scan[2];
+    // exact binning: the count pass keeps each (triangle, bin) pair's rank
+    // within its bin, so the fill pass stores every entry without atomics
+    uint32_t* ranks;           // rank_cap slots; a warp's walk owns a contiguous run
+    uint32_t* walk_base;       // first slot of each walk (walk = triangle slot / 32)
+    uint32_t* rank_next;       // slot reservation counter (a Ctl's rank_next)
+    unsigned long long rank_cap;
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -419,18 +428,21 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
 // belongs to the r-th non-empty range after the first, r = the starts at or
 // before it -- integer-pipe work, with one shared-memory load for the
 // owner's rectangle.  A lane takes up to kPairsPerLane pairs per pass and
-// issues their atomics back to back: the fill pass is bound by the latency
-// of its atomics with return, so several must be in flight per lane.
-// Mode 0: count (atomicAdd on counts), 1: fill (append entry), 2: predicted
-// fill (append within the bin's predicted capacity), 3: pre-pass count
-// (atomicAdd on the first feature slot).  One atomic per pair: grouping the
+// issues their atomics back to back: atomics with return are bound by their
+// latency, so several must be in flight per lane.
+// Mode 0: count (atomicAdd on counts; its return, the pair's rank within the
+// bin, is kept in the walk's rank slots), 1: fill (entry at the bin's offset
+// + rank: no atomics), 2: predicted fill (append within the bin's predicted
+// capacity), 3: pre-pass count (atomicAdd on the first feature slot).  A
+// walk is identified by `walk` (its first triangle slot / 32), so the count
+// and fill passes of the same triangles meet the same slots.  One atomic per pair: grouping the
 // lanes of a warp that hit the same bin (__match_any_sync, one atomic per
 // group) measured ~10% slower on GB300 for both the 1M soup and the 4K
 // icosphere, since same-bin lanes are rare and MATCH is costly.
 constexpr uint32_t kPairsPerLane = 4;
 
 template <int MODE>
-__device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid) {
+__device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid, uint32_t walk) {
     __shared__ uint4 s_tab[8][32];   // per warp: (first pair, width, bx0 | by0 << 16, entry) of each lane
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bx0 = rect.x & 0xFFFFu, bx1 = rect.x >> 16;
@@ -449,6 +461,18 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
     const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     if (total == 0u) return;   // warp-uniform
     const uint32_t excl = incl - n;
+    // exact binning: the walk's rank slots, reserved by the count pass and
+    // found again by the fill pass (same triangles, same enumeration)
+    uint32_t wb = 0;
+    if (MODE == 0) {
+        if (lane == 0) {
+            wb = atomicAdd(F.rank_next, total);
+            F.walk_base[walk] = wb;
+        }
+        wb = __shfl_sync(0xFFFFFFFFu, wb, 0);
+    } else if (MODE == 1) {
+        wb = __ldg(&F.walk_base[walk]);
+    }
     s_tab[warp][lane] = make_uint4(excl, w, bx0 | (by0 << 16), entry);
     __syncwarp();
     const uint32_t nonempty = __ballot_sync(0xFFFFFFFFu, n != 0u);
@@ -477,11 +501,29 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
             bin[u] = ((d.z & 0xFFFFu) + (j - q * d.y)) + ((d.z >> 16) + q) * F.nbx;
             ent[u] = d.w;
         }
-        if (MODE == 0 || MODE == 3) {
-            uint32_t* const tgt = MODE == 0 ? F.counts : F.feat;
+        if (MODE == 3) {
 #pragma unroll
             for (uint32_t u = 0; u < kPairsPerLane; ++u)
-                if (act[u]) atomicAdd(&tgt[bin[u]], 1u);
+                if (act[u]) atomicAdd(&F.feat[bin[u]], 1u);
+        } else if (MODE == 0) {
+            // count, keeping the pair's rank within its bin (slots past the
+            // storage are dropped: that frame overflows and is not filled)
+            uint32_t rank[kPairsPerLane];
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) rank[u] = act[u] ? atomicAdd(&F.counts[bin[u]], 1u) : 0u;
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) {
+                const unsigned long long slot = (unsigned long long)wb + base + u * 32u + lane;
+                if (act[u] && slot < F.rank_cap) F.ranks[slot] = rank[u];
+            }
+        } else if (MODE == 1) {
+            // fill: the bin's offset plus the rank the count pass kept
+            uint32_t rank[kPairsPerLane];
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) rank[u] = act[u] ? __ldg(&F.ranks[wb + base + u * 32u + lane]) : 0u;
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u)
+                if (act[u]) F.list[__ldg(&F.offsets[bin[u]]) + rank[u]] = ent[u];
         } else {
             uint32_t pos[kPairsPerLane];
 #pragma unroll
@@ -489,9 +531,8 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
 #pragma unroll
             for (uint32_t u = 0; u < kPairsPerLane; ++u) {
                 if (!act[u]) continue;
-                if (MODE == 1) F.list[pos[u]] = ent[u];
                 // cursors start at the bin's offset; the bin owns capacity[bin] slots
-                else if (pos[u] < __ldg(&F.offsets[bin[u]]) + __ldg(&F.capacity[bin[u]])) F.list[pos[u]] = ent[u];
+                if (pos[u] < __ldg(&F.offsets[bin[u]]) + __ldg(&F.capacity[bin[u]])) F.list[pos[u]] = ent[u];
                 else atomicOr(&F.ctl->pred_overflow, 1u);
             }
         }

@@ -86,6 +86,8 @@ struct gbr_renderer {
 
     gbr::TriSetup* d_setup = nullptr;
     uint2* d_rects = nullptr;
+    uint32_t* d_walk = nullptr;     // first rank slot of each 32-triangle walk
+    uint32_t* d_keys = nullptr;     // per-triangle depth-key bounds
     uint64_t tri_cap = 0;
 
     gbr::MeshDev* d_meshes = nullptr;

@@ -37,10 +37,36 @@ __device__ __forceinline__ uint32_t find_mesh(const FrameDev& F, uint32_t prim) 
 }
 
 // Vertex stage (positions), triangle assembly, cull, frustum reject, raster
+// Lower bound of the depth keys any fragment of the triangle can produce.
+// A pixel covered under the 16.16 rule is at most the snapping distance
+// outside the float triangle, so each float edge value there is at least
+// -beta with beta <= 3*2^-17*D + 2^-32 + 2^-20*D^2 (D = the triangle's
+// x + y extent; snapping moves vertices <= 2^-17 px; the float evaluation
+// errs by <= 4 ulp of its product terms), and the three edge values sum to
+// the float area within 2^-20*D^2 each.  With g = (2^-15*D + 2^-32 +
+// 2^-18*D^2)/area, every weight is >= -g and the weights sum to 1 +- g, so
+// z >= zmin*(1-g) - (3g + 2^-22)*max|z_i| when zmin >= 0 (2^-22 covers the
+// rounding of the fused z chain).  The key of that bound never exceeds the
+// key of a fragment of the triangle, so the triangle cannot win a pixel whose
+// stored key is below it.  0: no bound (float path, vertices behind z = 0);
+// 0x7FFFFFFF: every fragment has z >= 1 and loses everywhere.
+__device__ __forceinline__ uint32_t hiz_key(const TriSetup& t) {
+    if (t.flags & kFlagFloat) return 0u;
+    const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
+    if (!(zmin >= 0.f)) return 0u;
+    const float zabs = fmaxf(fabsf(t.z0), fmaxf(fabsf(t.z1), fabsf(t.z2)));
+    const float D = (max3f(t.x0, t.x1, t.x2) - min3f(t.x0, t.x1, t.x2)) + (max3f(t.y0, t.y1, t.y2) - min3f(t.y0, t.y1, t.y2)) + 1.f;
+    const float g = (D * 3.0517578125e-05f + 2.3283064365386963e-10f + D * D * 3.814697265625e-06f) * t.inv_area;
+    const float zb = zmin * (1.f - g) - (3.f * g + 2.384185791015625e-07f) * zabs;
+    if (!(zb > 0.f)) return 0u;
+    if (zb >= 1.f) return 0x7FFFFFFFu;
+    return (uint32_t)__float2int_rz(__fmul_rn(zb, 2147483648.0f));
+}
+
 // setup record and bin rectangle of triangle `prim`, then the count pass
 // (MODE 0) or the predicted-capacity fill (MODE 1).  Called by whole warps.
 template <int MODE>
-__device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim) {
+__device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim, uint32_t walk) {
     const bool in_range = prim < F.num_tris;
     uint2 rect = empty_rect();
     bool visible = false, fpath = false, no_raster = true;
@@ -104,6 +130,12 @@ __device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim) {
             rec[1] = make_uint4(__float_as_uint(s2.x), __float_as_uint(s2.y), __float_as_uint(nz[0]), __float_as_uint(nz[1]));
             rec[2] = make_uint4(__float_as_uint(nz[2]), __float_as_uint(inv_area), flags, mi);
             rect = pack_rect(r, no_raster);
+            // the raster depth-sorts a bin's triangles by this bound before it
+            // reads their records
+            TriSetup t;
+            t.x0 = s0.x; t.y0 = s0.y; t.x1 = s1.x; t.y1 = s1.y; t.x2 = s2.x; t.y2 = s2.y;
+            t.z0 = nz[0]; t.z1 = nz[1]; t.z2 = nz[2]; t.inv_area = inv_area; t.flags = flags; t.mesh = mi;
+            F.keys[prim] = hiz_key(t);
         }
         F.rects[prim] = rect;
     }
@@ -114,8 +146,8 @@ __device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim) {
         if (vis_mask) atomicAdd(&F.ctl->num_visible, (uint32_t)__popc(vis_mask));
         if (fp_mask) atomicAdd(&F.ctl->num_float_path, (uint32_t)__popc(fp_mask));
     }
-    if (MODE == 0) bin_walk<0>(F, rect, 0u, visible);
-    else bin_walk<2>(F, rect, prim | (no_raster ? kNoRasterBit : 0u), visible);
+    if (MODE == 0) bin_walk<0>(F, rect, 0u, visible, walk);
+    else bin_walk<2>(F, rect, prim | (no_raster ? kNoRasterBit : 0u), visible, walk);
 }
 
 template <int MODE>
@@ -127,23 +159,23 @@ __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
     // a resident grid strides over the triangles, so that a guarded launch
     // that does not run costs one wave of early exits
     for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x)
-        setup_tri<MODE>(F, base + threadIdx.x);
+        setup_tri<MODE>(F, base + threadIdx.x, (base + threadIdx.x) >> 5);
     pdl_release();
 }
 
 // Second pass of exact binning for triangle `prim`.  Called by whole warps.
-__device__ __forceinline__ void fill_tri(const FrameDev& F, uint32_t prim) {
+__device__ __forceinline__ void fill_tri(const FrameDev& F, uint32_t prim, uint32_t walk) {
     const bool in_range = prim < F.num_tris;
     const uint2 rect = in_range ? F.rects[prim] : empty_rect();
     const uint32_t entry = prim | ((rect.y & 0x80000000u) ? kNoRasterBit : 0u);
-    bin_walk<1>(F, rect, entry, in_range);
+    bin_walk<1>(F, rect, entry, in_range, walk);
 }
 
 __global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
     pdl_wait();
     if (F.ctl->overflow || (F.exact_guard && !F.ctl->pred_overflow)) return;
     for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x)
-        fill_tri(F, base + threadIdx.x);
+        fill_tri(F, base + threadIdx.x, (base + threadIdx.x) >> 5);
     pdl_release();
 }
 
@@ -151,49 +183,19 @@ __global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
 // Raster + ROP + shade
 // ---------------------------------------------------------------------------
 struct RasterShared {
-    TriSetup rec[kBatch];
-    uint32_t prim[kBatch];
+    TriSetup rec[kMaxPhase];     // setup records of the running phase
+    uint32_t prim[kBatch];       // staged bin entries (rasterisable triangles)
+    uint32_t key[kBatch];        // their depth-key lower bounds
+    uint16_t order[kBatch];      // staged triangles, front to back by depth bucket
+    uint32_t bucket[kDepthBuckets];   // counts -> starts -> (after the scatter) ends
     uint32_t warp_count[kRasterThreads / 32];
     uint32_t warp_max[kRasterThreads / 32];
     uint32_t item[4];
     int next;
-    int nv;
-    int last;
-    uint32_t tile_max;   // max depth key over the tile's pixels (0xFFFFFFFF while any pixel is empty)
-    uint32_t key[kBatch];        // depth-key lower bound of each staged triangle
-    uint16_t order[kBatch];      // staged triangles, front to back by 16 key buckets
-    uint32_t bcount[16];
-    uint32_t bstart[17];         // after the scatter: bstart[b] = end of bucket b
     uint32_t scene_next;         // batch: scene of the fetched work item
     uint32_t scene_loaded;       // batch: scene whose descriptor `frame` holds
     __align__(16) FrameDev frame;
 };
-
-// Lower bound of the depth keys any fragment of the triangle can produce.
-// A pixel covered under the 16.16 rule is at most the snapping distance
-// outside the float triangle, so each float edge value there is at least
-// -beta with beta <= 3*2^-17*D + 2^-32 + 2^-20*D^2 (D = the triangle's
-// x + y extent; snapping moves vertices <= 2^-17 px; the float evaluation
-// errs by <= 4 ulp of its product terms), and the three edge values sum to
-// the float area within 2^-20*D^2 each.  With g = (2^-15*D + 2^-32 +
-// 2^-18*D^2)/area, every weight is >= -g and the weights sum to 1 +- g, so
-// z >= zmin*(1-g) - (3g + 2^-22)*max|z_i| when zmin >= 0 (2^-22 covers the
-// rounding of the fused z chain).  The key of that bound never exceeds the
-// key of a fragment of the triangle, so the triangle cannot win a pixel whose
-// stored key is below it.  0: no bound (float path, vertices behind z = 0);
-// 0x7FFFFFFF: every fragment has z >= 1 and loses everywhere.
-__device__ __forceinline__ uint32_t hiz_key(const TriSetup& t) {
-    if (t.flags & kFlagFloat) return 0u;
-    const float zmin = fminf(t.z0, fminf(t.z1, t.z2));
-    if (!(zmin >= 0.f)) return 0u;
-    const float zabs = fmaxf(fabsf(t.z0), fmaxf(fabsf(t.z1), fabsf(t.z2)));
-    const float D = (max3f(t.x0, t.x1, t.x2) - min3f(t.x0, t.x1, t.x2)) + (max3f(t.y0, t.y1, t.y2) - min3f(t.y0, t.y1, t.y2)) + 1.f;
-    const float g = (D * 3.0517578125e-05f + 2.3283064365386963e-10f + D * D * 3.814697265625e-06f) * t.inv_area;
-    const float zb = zmin * (1.f - g) - (3.f * g + 2.384185791015625e-07f) * zabs;
-    if (!(zb > 0.f)) return 0u;
-    if (zb >= 1.f) return 0x7FFFFFFFu;
-    return (uint32_t)__float2int_rz(__fmul_rn(zb, 2147483648.0f));
-}
 
 __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
                                              int ty0, int tw, int th, uint32_t lane) {
@@ -242,7 +244,7 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
 }
 
 // Triangles outside the guard band: the reference's float edge functions.
-__device__ __forceinline__ void raster_float(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
+__device__ __noinline__ void raster_float(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
                                              int ty0, int tw, int th, uint32_t lane) {
     const float x0 = t.x0, y0 = t.y0, x1 = t.x1, y1 = t.y1, x2 = t.x2, y2 = t.y2;
     if (x0 != x0 || y0 != y0 || x1 != x1 || y1 != y1 || x2 != x2 || y2 != y2) return;
@@ -311,7 +313,8 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
     if (Q->overflow) return;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t num_items = Q->num_items;
-    const uint32_t phase = (BATCH ? B.phase : F.phase) ? (BATCH ? B.phase : F.phase) : kPhase;
+    const uint32_t phase_req = BATCH ? B.phase : F.phase;
+    const uint32_t phase = phase_req == 0u ? kPhase : min(phase_req, kMaxPhase);
     if (BATCH && tid == 0) S.scene_loaded = 0xFFFFFFFFu;
     for (;;) {
         if (tid == 0) {
@@ -347,63 +350,78 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
         unsigned long long* const gvis = G.gvis;
         const uint32_t width = G.width;
         for (int i = (int)tid; i < npx; i += kRasterThreads) tile[i] = kEmptyVis;
+        const uint32_t* const keys = G.keys;
         for (uint32_t b0 = 0; b0 < count && npx > 0; b0 += kBatch) {
-            __syncthreads();
+            // stage the entries with their depth-key bounds (no setup record
+            // is read before a triangle's phase comes) and count the
+            // rasterisable ones per depth bucket
+            constexpr uint32_t kPer = kBatch / kRasterThreads;
+            static_assert(kDepthBuckets == kRasterThreads, "one bucket per thread");
             const uint32_t n = min((uint32_t)kBatch, count - b0);
-            const uint32_t e = tid < n ? __ldg(list + start + b0 + tid) : kNoRasterBit;
-            const bool keep = !(e & kNoRasterBit);
-            const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
-            if (lane == 0) S.warp_count[warp] = (uint32_t)__popc(bal);
-            if (tid == 0) S.next = 0;
+            __syncthreads();   // the previous batch is done with the shared arrays
+            S.bucket[tid] = 0u;
             __syncthreads();
-            uint32_t base = 0, total = 0;
+#pragma unroll 4
+            for (uint32_t j = 0; j < kPer; ++j) {
+                const uint32_t idx = j * kRasterThreads + tid;
+                const uint32_t e = idx < n ? __ldg(list + start + b0 + idx) : kNoRasterBit;
+                const bool keep = !(e & kNoRasterBit);
+                const uint32_t k = keep ? __ldg(keys + e) : 0u;
+                S.prim[idx] = e;
+                S.key[idx] = k;
+                if (keep) atomicAdd(&S.bucket[k >> 23], 1u);
+            }
+            __syncthreads();
+            // bucket starts: exclusive scan of the 256 counts; their sum is the
+            // number of staged triangles
+            uint32_t total = 0;
+            {
+                const uint32_t c = S.bucket[tid];
+                uint32_t x = c;
 #pragma unroll
-            for (uint32_t w = 0; w < kRasterThreads / 32; ++w) {
-                const uint32_t c = S.warp_count[w];
-                base += w < warp ? c : 0u;
-                total += c;
-            }
-            if (keep) {
-                const uint32_t pos = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
-                const uint4* rp = reinterpret_cast<const uint4*>(setup) + 3u * e;
-                uint4* dst = reinterpret_cast<uint4*>(&S.rec[pos]);
-                dst[0] = __ldg(rp);
-                dst[1] = __ldg(rp + 1);
-                dst[2] = __ldg(rp + 2);
-                S.prim[pos] = e;
-            }
-            __syncthreads();
-            // front-to-back order: a counting sort of the staged triangles by
-            // the top 4 bits of their depth-key lower bound
-            if (tid < 16) S.bcount[tid] = 0u;
-            __syncthreads();
-            uint32_t bk = 0;
-            if (tid < total) {
-                const uint32_t kb = hiz_key(S.rec[tid]);
-                S.key[tid] = kb;
-                bk = kb >> 27;
-                atomicAdd(&S.bcount[bk], 1u);
+                for (uint32_t d = 1; d < 32; d <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, x, d);
+                    if (lane >= d) x += t;
+                }
+                if (lane == 31u) S.warp_count[warp] = x;
+                __syncthreads();
+                uint32_t before = 0;
+#pragma unroll
+                for (uint32_t w = 0; w < kRasterThreads / 32; ++w) {
+                    const uint32_t wc = S.warp_count[w];
+                    before += w < warp ? wc : 0u;
+                    total += wc;
+                }
+                S.bucket[tid] = before + x - c;
             }
             __syncthreads();
-            if (tid == 0) {
-                uint32_t a = 0;
-                for (int b = 0; b < 16; ++b) { S.bstart[b] = a; a += S.bcount[b]; }
-                S.bstart[16] = a;
+#pragma unroll
+            for (uint32_t j = 0; j < kPer; ++j) {
+                const uint32_t idx = j * kRasterThreads + tid;
+                if (idx < n && !(S.prim[idx] & kNoRasterBit))
+                    S.order[atomicAdd(&S.bucket[S.key[idx] >> 23], 1u)] = (uint16_t)idx;
             }
-            __syncthreads();
-            if (tid < total) S.order[atomicAdd(&S.bstart[bk], 1u)] = (uint16_t)tid;
-            __syncthreads();
+            // now S.bucket[b] = end of bucket b
             // phases of `phase` triangles; the tile's max depth key is refreshed
             // between phases.  A triangle whose key bound exceeds it cannot win
             // a pixel; once a whole bucket's lower bound does, the rest of the
             // batch is skipped.
             for (uint32_t p0 = 0; p0 < total; p0 += phase) {
+                __syncthreads();   // the order, or the previous phase's records and tile
                 if (b0 > 0 || p0 > 0) {
                     uint32_t m = 0;
                     for (int i = (int)tid; i < npx; i += kRasterThreads)
                         m = max(m, (uint32_t)(tile[i] >> 32));
                     m = __reduce_max_sync(0xFFFFFFFFu, m);
                     if (lane == 0) S.warp_max[warp] = m;
+                }
+                // the phase's setup records, 16 bytes per thread
+                const uint32_t pn = min(phase, total - p0);
+                // (triangle k's record goes to slot k mod kMaxPhase: phase <= kMaxPhase)
+                for (uint32_t r = tid; r < 3u * pn; r += kRasterThreads) {
+                    const uint32_t q = r / 3u, k = p0 + q;
+                    const uint4* rp = reinterpret_cast<const uint4*>(setup) + 3u * S.prim[S.order[k]];
+                    reinterpret_cast<uint4*>(&S.rec[k & (kMaxPhase - 1u)])[r - 3u * q] = __ldg(rp + (r - 3u * q));
                 }
                 if (tid == 0) S.next = (int)p0;
                 __syncthreads();
@@ -413,8 +431,8 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
 #pragma unroll
                     for (uint32_t w = 0; w < kRasterThreads / 32; ++w) tile_max = max(tile_max, S.warp_max[w]);
                 }
-                // buckets [0, tile_max >> 27] can still hold a winner
-                const uint32_t limit = tile_max >= 0x80000000u ? total : S.bstart[tile_max >> 27];
+                // buckets [0, tile_max >> 23] can still hold a winner
+                const uint32_t limit = tile_max >= 0x80000000u ? total : S.bucket[tile_max >> 23];
                 if (p0 >= limit) break;   // uniform: every thread sees the same tile_max
                 const uint32_t p1 = min(limit, p0 + phase);
                 for (;;) {
@@ -424,11 +442,10 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                     if (k >= (int)p1) break;
                     const uint32_t i = S.order[k];
                     if (S.key[i] > tile_max) continue;
-                    const TriSetup& t = S.rec[i];
+                    const TriSetup& t = S.rec[(uint32_t)k & (kMaxPhase - 1u)];
                     if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
                     else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
                 }
-                __syncthreads();
             }
         }
         __syncthreads();
@@ -515,7 +532,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
     __shared__ __align__(16) FrameDev sF;
     __shared__ uint32_t s_sc;
     const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
-    setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x);
+    setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x, (blockIdx.x * 256u + threadIdx.x) >> 5);
 }
 
 __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
@@ -523,7 +540,7 @@ __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
     __shared__ __align__(16) FrameDev sF;
     __shared__ uint32_t s_sc;
     const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
-    fill_tri(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x);
+    fill_tri(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x, (blockIdx.x * 256u + threadIdx.x) >> 5);
 }
 
 __global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {

@@ -58,7 +58,10 @@ constexpr size_t kOffIds = kOffGvis + align256(size_t(kNaMaxPixels) * 8u);
 constexpr size_t kOffCtl = kOffIds + align256(size_t(kNaMaxPixels) * 4u);
 constexpr size_t kOffMesh = kOffCtl + align256(sizeof(Ctl));
 constexpr size_t kOffScan = kOffMesh + align256(sizeof(MeshDev));
-constexpr size_t kScratchBytes = kOffScan + align256(scan_state_bytes(kNaMaxBins));
+constexpr size_t kOffRanks = kOffScan + align256(scan_state_bytes(kNaMaxBins));
+constexpr size_t kOffWalk = kOffRanks + align256(size_t(kNaMaxPairs) * 4u);
+constexpr size_t kOffKeys = kOffWalk + align256(size_t(kNaMaxTris / 32u + 8u) * 4u);
+constexpr size_t kScratchBytes = kOffKeys + align256(size_t(kNaMaxTris) * 4u);
 
 // The only device memory this entry point uses besides the caller's.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -170,6 +173,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.meshes = reinterpret_cast<const MeshDev*>(b + kOffMesh);
     F.setup = reinterpret_cast<TriSetup*>(b + kOffSetup);
     F.rects = reinterpret_cast<uint2*>(b + kOffRects);
+    F.keys = reinterpret_cast<uint32_t*>(b + kOffKeys);
     F.counts = reinterpret_cast<uint32_t*>(b + kOffCounts);
     F.offsets = reinterpret_cast<uint32_t*>(b + kOffOffsets);
     F.cursors = reinterpret_cast<uint32_t*>(b + kOffCursors);
@@ -183,6 +187,10 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.ids = reinterpret_cast<uint32_t*>(b + kOffIds);
     F.ctl = reinterpret_cast<Ctl*>(b + kOffCtl);
     F.scan_state = reinterpret_cast<ScanState*>(b + kOffScan);
+    F.ranks = reinterpret_cast<uint32_t*>(b + kOffRanks);
+    F.rank_cap = kNaMaxPairs;
+    F.walk_base = reinterpret_cast<uint32_t*>(b + kOffWalk);
+    F.rank_next = &reinterpret_cast<Ctl*>(b + kOffCtl)->rank_next;
     F.colour = d_colour;
     F.depth = d_depth;
 

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) prepass_kernel(FrameDev F) {
         atomicMax(&F.feat[5u * nb + cbin], ordered(zc));
     }
     // sampled (triangle, bin) pairs
-    bin_walk<3>(F, visible ? pack_rect(r, false) : empty_rect(), 0u, visible);
+    bin_walk<3>(F, visible ? pack_rect(r, false) : empty_rect(), 0u, visible, 0u);
 }
 
 // The kFeatures features of bin b (shared by inference and training data).

@@ -172,7 +172,7 @@ gbr_status gbr_set_lights(gbr_renderer *r, const gbr_light *lights, uint32_t n);
 /* Binning method for the following frames. */
 gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
 /* Raster tuning (no counterpart in the reference; used by the autotuner):
- * phase = triangles rasterised between hierarchical-z refreshes (0: 16),
+ * phase = triangles rasterised between hierarchical-z refreshes, 0..64 (0: 16),
  * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
 gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
 /* Record CUDA-event times into gbr_stats (off by default).
@@ -221,7 +221,7 @@ typedef struct {
     uint32_t bin_size;     /* bins of bin_size x bin_size pixels, 1..64 */
     uint32_t queue_chunk;  /* bin-list entries per raster work item, >= 1 */
     uint32_t raster_ctas;  /* raster variant: CTAs per SM, 2..6 (0: 6) */
-    uint32_t raster_phase; /* triangles between hierarchical-z refreshes (0: 16) */
+    uint32_t raster_phase; /* triangles between hierarchical-z refreshes, 0..64 (0: 16) */
 } gbr_batch_config;
 typedef struct {
     uint32_t num_scenes;
