@@ -142,6 +142,7 @@ void free_bins(gbr_renderer* r) {
     r->d_items = nullptr;
     r->items_cap = 0;
     r->list_cap = 0;
+    r->seen_pairs = r->seen_visible = 0;
 }
 
 gbr_status ensure_list(gbr_renderer* r, uint64_t pairs) {
@@ -154,7 +155,8 @@ gbr_status ensure_list(gbr_renderer* r, uint64_t pairs) {
     cudaFree(r->d_items);
     r->d_list = nullptr;
     r->d_items = nullptr;
-    const uint64_t items = (uint64_t)nb + cap / r->chunk + 1u;
+    // work items of up to queue_chunk entries, as short as kMinChunk
+    const uint64_t items = (uint64_t)nb + cap / std::min(r->chunk, kMinChunk) + 1u;
     // the bin list, then as many rank slots (exact binning's count pass)
     if (cudaMalloc(&r->d_list, 2u * cap * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&r->d_items, items * sizeof(uint4)) != cudaSuccess) {
@@ -248,8 +250,20 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     FrameDev F;
     frame_basics(r, cam, cull, sample, vis, F);
     F.nbx = r->nbx; F.nby = r->nby; F.bw = r->bw; F.bh = r->bh; F.num_bins = nb;
+    // raster work: once a frame has been seen, items hold about half of a
+    // raster CTA's share of the pairs (so a few crowded bins do not
+    // serialise the frame), within [kMinChunk, queue_chunk]; and with the
+    // library's phase, triangles spanning under 4 bins on average (little
+    // overdraw per bin) refresh the tile's depth bound every kMaxPhase
+    // triangles rather than every kPhase
     F.chunk = r->chunk;
     F.phase = r->raster_phase;
+    if (r->seen_pairs) {
+        const uint64_t grid = (uint64_t)r->num_sms * (uint64_t)std::max(r->raster_blocks_per_sm, 1);
+        const uint64_t share = r->seen_pairs / (2u * grid);
+        F.chunk = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(share, r->chunk), std::min(r->chunk, kMinChunk));
+        if (F.phase == 0u) F.phase = r->seen_pairs < 4u * r->seen_visible ? kMaxPhase : kPhase;
+    }
     F.raster_ctas = r->raster_ctas;
     F.meshes = r->d_meshes;
     F.setup = r->d_setup; F.rects = r->d_rects; F.keys = r->d_keys;
@@ -330,6 +344,8 @@ gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
         GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(r->nbx * r->nby)));
         return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the frame is invalid");
     }
+    r->seen_pairs = r->h_ctl->num_pairs;
+    r->seen_visible = r->h_ctl->num_visible;
     // predicted capacities that did not fit the list: grow it for the next
     // frames, within reason (the frame itself was re-binned exactly)
     const uint64_t want = r->h_ctl->pred_capacity;

@@ -26,6 +26,7 @@ constexpr int kBatch = 2048;                      // bin entries the raster dept
 constexpr int kDepthBuckets = 256;                // front-to-back buckets: top 8 bits of the depth key
 constexpr uint32_t kPhase = 16;                   // triangles between hierarchical-z refreshes
 constexpr uint32_t kMaxPhase = 64;                // setup records staged per phase
+constexpr uint32_t kMinChunk = 64;                // smallest raster work item the library picks
 constexpr uint32_t kDefaultRasterCtas = 6;        // raster_kernel variant (CTAs per SM) used by default
 
 enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
@@ -435,10 +436,10 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
 // + rank: no atomics), 2: predicted fill (append within the bin's predicted
 // capacity), 3: pre-pass count (atomicAdd on the first feature slot).  A
 // walk is identified by `walk` (its first triangle slot / 32), so the count
-// and fill passes of the same triangles meet the same slots.  One atomic per pair: grouping the
-// lanes of a warp that hit the same bin (__match_any_sync, one atomic per
-// group) measured ~10% slower on GB300 for both the 1M soup and the 4K
-// icosphere, since same-bin lanes are rare and MATCH is costly.
+// and fill passes of the same triangles meet the same slots.  One atomic per
+// pair: merging the atomics of same-bin lanes -- every such lane of the warp
+// (__match_any_sync) or runs of neighbouring lanes -- measured 8-10% slower
+// on GB300 for both the 1M soup and the 4K icosphere.
 constexpr uint32_t kPairsPerLane = 4;
 
 template <int MODE>

@@ -55,6 +55,9 @@ struct gbr_renderer {
     int raster_blocks_per_sm = 1;
     uint32_t raster_phase = 0;   // 0: library default
     uint32_t raster_ctas = 0;    // 0: library default
+    // the last finished frame's pair and visible-triangle counts: they size
+    // the next frames' raster work items and phases (0: none seen yet)
+    uint64_t seen_pairs = 0, seen_visible = 0;
 
     // predicted-capacity binning
     uint32_t* d_feat = nullptr;

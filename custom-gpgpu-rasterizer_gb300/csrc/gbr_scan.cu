@@ -37,9 +37,9 @@ __device__ __forceinline__ uint32_t bin_size(const ScanDev& S, uint32_t b) {
     }
 }
 
-__device__ __forceinline__ uint32_t bin_items(uint32_t c, uint32_t chunk) {
-    return c == 0u ? 1u : (c + chunk - 1u) / chunk;
-}
+// Raster work items of a bin of c entries (an empty bin has none: its pixels
+// stay empty in the merge buffer and shade to the clear colour).
+__device__ __forceinline__ uint32_t bin_items(uint32_t c, uint32_t chunk) { return (c + chunk - 1u) / chunk; }
 
 __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
