@@ -68,8 +68,10 @@ __device__ __forceinline__ uint32_t hiz_key(const TriSetup& t) {
 // Vertex stage (positions), triangle assembly, cull, frustum reject, raster
 // setup record, depth-key bound and bin rectangle of triangle `prim`, then the count pass
 // (MODE 0) or the predicted-capacity fill (MODE 1).  Called by whole warps.
+// Returns the warp's visible and float-path triangle counts (bits 0-15 and
+// 16-31), for the block's statistics.
 template <int MODE>
-__device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim, uint32_t walk) {
+__device__ __forceinline__ uint32_t setup_tri(const FrameDev& F, uint32_t prim, uint32_t walk) {
     const bool in_range = prim < F.num_tris;
     uint2 rect = empty_rect();
     bool visible = false, fpath = false, no_raster = true;
@@ -142,15 +144,29 @@ __device__ __forceinline__ void setup_tri(const FrameDev& F, uint32_t prim, uint
         }
         F.rects[prim] = rect;
     }
-    // frame statistics, one atomic per warp
-    const unsigned vis_mask = __ballot_sync(0xFFFFFFFFu, visible);
-    const unsigned fp_mask = __ballot_sync(0xFFFFFFFFu, fpath);
-    if (lane_id() == 0) {
-        if (vis_mask) atomicAdd(&F.ctl->num_visible, (uint32_t)__popc(vis_mask));
-        if (fp_mask) atomicAdd(&F.ctl->num_float_path, (uint32_t)__popc(fp_mask));
-    }
+    const uint32_t counts = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, visible)) |
+                            ((uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, fpath)) << 16);
     if (MODE == 0) bin_walk<0>(F, rect, 0u, visible, walk);
     else bin_walk<2>(F, rect, prim | (no_raster ? kNoRasterBit : 0u), visible, walk);
+    return counts;
+}
+
+// Frame statistics of a block: its warps' counts, summed in shared memory,
+// then one atomic per counter and block (not per warp: every warp of the
+// grid adding to the same two words serialises at one L2 slice).
+__device__ __forceinline__ void add_block_stats(Ctl* ctl, uint32_t warp_vis, uint32_t warp_fp) {
+    __shared__ uint32_t s_vis, s_fp;
+    if (threadIdx.x == 0) { s_vis = 0u; s_fp = 0u; }
+    __syncthreads();
+    if ((threadIdx.x & 31u) == 0u) {
+        if (warp_vis) atomicAdd(&s_vis, warp_vis);
+        if (warp_fp) atomicAdd(&s_fp, warp_fp);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (s_vis) atomicAdd(&ctl->num_visible, s_vis);
+        if (s_fp) atomicAdd(&ctl->num_float_path, s_fp);
+    }
 }
 
 template <int MODE>
@@ -161,8 +177,13 @@ __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
     if (MODE == 0 ? (F.exact_guard && !F.ctl->pred_overflow) : (F.ctl->pred_overflow != 0u)) return;
     // a resident grid strides over the triangles, so that a guarded launch
     // that does not run costs one wave of early exits
-    for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x)
-        setup_tri<MODE>(F, base + threadIdx.x, (base + threadIdx.x) >> 5);
+    uint32_t vis = 0, fp = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x) {
+        const uint32_t c = setup_tri<MODE>(F, base + threadIdx.x, (base + threadIdx.x) >> 5);
+        vis += c & 0xFFFFu;
+        fp += c >> 16;
+    }
+    add_block_stats(F.ctl, vis, fp);
     pdl_release();
 }
 
@@ -559,7 +580,9 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
     __shared__ __align__(16) FrameDev sF;
     __shared__ uint32_t s_sc;
     const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
-    setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x, (blockIdx.x * 256u + threadIdx.x) >> 5);
+    const uint32_t c = setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x,
+                                    (blockIdx.x * 256u + threadIdx.x) >> 5);
+    add_block_stats(sF.ctl, c & 0xFFFFu, c >> 16);
 }
 
 __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {

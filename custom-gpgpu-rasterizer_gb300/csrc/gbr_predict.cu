@@ -151,8 +151,14 @@ __global__ void __launch_bounds__(256) prepass_kernel(FrameDev F) {
             if (!(zc == zc)) zc = 0.f;
         }
     }
+    // sampled visible triangles: one atomic per block
+    __shared__ uint32_t s_sampled;
+    if (threadIdx.x == 0) s_sampled = 0u;
+    __syncthreads();
     const unsigned vis = __ballot_sync(0xFFFFFFFFu, visible);
-    if (lane == 0 && vis) atomicAdd(&F.ctl->num_sampled, (uint32_t)__popc(vis));
+    if (lane == 0 && vis) atomicAdd(&s_sampled, (uint32_t)__popc(vis));
+    __syncthreads();
+    if (threadIdx.x == 0 && s_sampled) atomicAdd(&F.ctl->num_sampled, s_sampled);
     const uint32_t nb = F.num_bins;
     if (visible) {
         atomicAdd(&F.feat[1u * nb + cbin], 1u);
