@@ -463,7 +463,7 @@ def run_batch(args, rank, world, local):
         b.add_scene(r, s)
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
-        best = b.autotune(bin_sizes=(8, 16, 32), chunks=(32, 64, 128), raster_ctas=(4, 5, 6), frames=2, stream=sptr)
+        best = b.autotune(bin_sizes=(8, 16, 32), chunks=(128, 512, 2048), raster_ctas=(5, 6), frames=2, stream=sptr)
     t_tune = time.perf_counter() - t0
     b.set_timing(True)
     with torch.cuda.stream(stream):

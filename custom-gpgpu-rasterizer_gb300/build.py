@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbr.so")
-SOURCES = ["gbr_kernels.cu", "gbr_scan.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_predict.cu"]
+SOURCES = ["gbr_kernels.cu", "gbr_scan.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_predict.cu", "gbr_obj.cpp"]
 HEADERS = ["gbr_device.cuh", "gbr_shade.cuh", "gbr_kernels.h", "gbr_predict.h", "gbr_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -52,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         common += ["-Xptxas", "-v"]
     procs, objs = [], []
     for src in SOURCES:
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         procs.append((src, subprocess.Popen(common + ["-c", os.path.join(CSRC, src), "-o", obj],
                                             stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))

@@ -37,7 +37,8 @@ EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "g
             "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
             "gbr_batch_set_view", "gbr_batch_set_config", "gbr_batch_get_config", "gbr_batch_autotune",
             "gbr_batch_set_timing", "gbr_batch_render", "gbr_batch_get_stats", "gbr_batch_scene_bins",
-            "gbr_batch_readback", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_last_error_string", "gbr_version"]
+            "gbr_batch_readback", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_obj_read_file", "gbr_obj_read_text",
+            "gbr_obj_free", "gbr_last_error_string", "gbr_version"]
 
 
 class GbrError(RuntimeError):
@@ -61,6 +62,11 @@ class Stats(C.Structure):
 
 class Light(C.Structure):
     _fields_ = [("type", C.c_uint32), ("colour", C.c_float * 3), ("intensity", C.c_float), ("vec", C.c_float * 3)]
+
+
+class ObjMesh(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("indices", C.c_void_p), ("num_vertices", C.c_uint32),
+                ("num_indices", C.c_uint32), ("num_faces", C.c_uint32), ("vertex_type", C.c_int32)]
 
 
 class BatchConfig(C.Structure):
@@ -132,6 +138,8 @@ def lib():
             "gbr_batch_scene_bins": [vp, u32, C.POINTER(u32), C.POINTER(u32)],
             "gbr_batch_readback": [vp, u32, vp, vp, vp, vp],
             "gbr_batch_get_bins": [vp, u32, vp, vp, u64, C.POINTER(u64), vp],
+            "gbr_obj_read_file": [C.c_char_p, C.c_int, C.POINTER(ObjMesh)],
+            "gbr_obj_read_text": [C.c_char_p, C.c_size_t, C.c_int, C.POINTER(ObjMesh)],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -141,6 +149,8 @@ def lib():
         L.gbr_last_error_string.argtypes = []
         L.gbr_version.restype = C.c_uint32
         L.gbr_version.argtypes = []
+        L.gbr_obj_free.restype = None
+        L.gbr_obj_free.argtypes = [C.POINTER(ObjMesh)]
         L.gbr_mlp_num_params.restype = C.c_uint32
         L.gbr_mlp_num_params.argtypes = []
         _LIB = L
@@ -150,6 +160,28 @@ def lib():
 def check(status: int):
     if status != GBR_OK:
         raise GbrError(status, lib().gbr_last_error_string().decode(errors="replace"))
+
+
+def read_obj(source, invert_y: bool = False, text: bool = False):
+    """ObjParser::ReadFromObjFile (ObjParser.cpp) through gbr_obj_read_file, or
+    gbr_obj_read_text when `text` (source: str or bytes).  Returns
+    (vertices: float32 (n, 14) IVertex rows [p3 uv2 n3 tan3 c3], indices:
+    uint32, vertex type: GBR_VT_* flags, faces read)."""
+    L = lib()
+    m = ObjMesh()
+    if text:
+        data = source.encode() if isinstance(source, str) else bytes(source)
+        check(L.gbr_obj_read_text(data, len(data), 1 if invert_y else 0, C.byref(m)))
+    else:
+        check(L.gbr_obj_read_file(os.fsencode(source), 1 if invert_y else 0, C.byref(m)))
+    try:
+        nv, ni = m.num_vertices, m.num_indices
+        verts = np.ctypeslib.as_array(C.cast(m.vertices, C.POINTER(C.c_float)), shape=(max(nv, 1) * 14,))
+        verts = verts[:nv * 14].reshape(nv, 14).copy()
+        idx = np.ctypeslib.as_array(C.cast(m.indices, C.POINTER(C.c_uint32)), shape=(max(ni, 1),))[:ni].copy()
+        return verts, idx, int(m.vertex_type), int(m.num_faces)
+    finally:
+        L.gbr_obj_free(C.byref(m))
 
 
 def _ptr(a: Optional[np.ndarray]):
@@ -385,7 +417,7 @@ class Batch:
         check(self._lib.gbr_batch_get_config(self.h, C.byref(cfg)))
         return {k: getattr(cfg, k) for k, _ in BatchConfig._fields_}
 
-    def autotune(self, bin_sizes=(8, 16, 32), chunks=(32, 64, 128), raster_ctas=None, frames: int = 2,
+    def autotune(self, bin_sizes=(8, 16, 32), chunks=(128, 512, 2048), raster_ctas=None, frames: int = 2,
                  stream: int = 0) -> dict:
         b, nb = _u32_list(bin_sizes)
         c, nc = _u32_list(chunks)

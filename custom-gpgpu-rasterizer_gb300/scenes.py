@@ -203,6 +203,72 @@ def sphere_scene(width: int = 640, height: int = 480, bin_size: int = 16, lon: i
                  sample=sample, vis=vis)
 
 
+def obj_sphere_text(lon: int = 48, lat: int = 24, radius: float = 1.0, bumps: float = 0.04, seed: int = 5) -> str:
+    """A Wavefront OBJ text (3ds Max style, as the reference's parser reads
+    it: "v  x y z", "f v/vt/vn ...") of a bumpy UV sphere: positions shared
+    across the uv seam, a uv grid with a seam column, one normal per
+    position, two triangles per quad (counter-clockwise from outside)."""
+    rng = np.random.default_rng(seed)
+    lines = ["# sphere written by scenes.obj_sphere_text", "o Sphere"]
+    pos = []
+    for j in range(lat + 1):
+        th = np.pi * j / lat
+        for i in range(lon):
+            ph = 2.0 * np.pi * i / lon
+            r = radius * (1.0 + bumps * float(rng.uniform(-1.0, 1.0)) * (0 < j < lat))
+            pos.append((r * np.sin(th) * np.cos(ph), r * np.cos(th), r * np.sin(th) * np.sin(ph)))
+    lines += ["v  %.6f %.6f %.6f" % p for p in pos]
+    lines += ["vt %.6f %.6f 0.000000" % (i / lon, j / lat) for j in range(lat + 1) for i in range(lon + 1)]
+    for p in pos:
+        n = np.asarray(p) / max(np.linalg.norm(p), 1e-12)
+        lines.append("vn %.6f %.6f %.6f" % tuple(n))
+    for j in range(lat):
+        for i in range(lon):
+            a, b = j * lon + i, j * lon + (i + 1) % lon
+            c, d = (j + 1) * lon + i, (j + 1) * lon + (i + 1) % lon
+            ta, tb = j * (lon + 1) + i, j * (lon + 1) + i + 1
+            tc, td = (j + 1) * (lon + 1) + i, (j + 1) * (lon + 1) + i + 1
+            corner = lambda v, t: "%d/%d/%d" % (v + 1, t + 1, v + 1)
+            lines.append("f %s %s %s " % (corner(a, ta), corner(c, tc), corner(b, tb)))
+            lines.append("f %s %s %s " % (corner(b, tb), corner(c, tc), corner(d, td)))
+    return "\n".join(lines) + "\n"
+
+
+def ivertex_array(rows: np.ndarray) -> np.ndarray:
+    """(n, 14) float32 rows [p3 uv2 n3 tan3 c3] -> IVERTEX56 records."""
+    rows = np.ascontiguousarray(rows, dtype=np.float32)
+    return rows.view(IVERTEX56).reshape(-1)
+
+
+def bump_normal_texture(size: int = 256, cells: int = 16) -> np.ndarray:
+    """A tangent-space normal map with tilted stripes, so the shader's TBN
+    transform (ShadePixelSafe, CUDAROPs.cu:429-435) changes the lighting."""
+    y, x = np.mgrid[0:size, 0:size]
+    t = np.sin(2.0 * np.pi * cells * (x + 0.5 * y) / size)
+    nx, ny, nz = 0.45 * t, 0.2 * np.cos(2.0 * np.pi * cells * y / size), np.ones_like(t)
+    n = np.stack([nx, ny, nz], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    c = np.clip(np.round((n * 0.5 + 0.5) * 255.0), 0, 255).astype(np.uint32)
+    return c[..., 0] | (c[..., 1] << 8) | (c[..., 2] << 16) | np.uint32(255 << 24)
+
+
+def obj_scene(vertices: np.ndarray, indices: np.ndarray, width: int = 800, height: int = 600,
+              bin_size: int = 16, sample: int = SAMPLE_POINT, vis: int = VIS_PBR, tex_size: int = 256) -> Scene:
+    """A mesh read by the OBJ reader (vertices as (n, 14) rows, uv + normal +
+    tangent) with all four maps bound -- checker diffuse, a non-flat normal
+    map, a striped specular map and a grey gloss map -- so every term of the
+    reference's Phong branch (ShadePixelSafe, CUDAROPs.cu:411-470) and its
+    tangent frame are exercised; camera 3 units away, 60 deg."""
+    mesh = Mesh(ivertex_array(vertices), np.ascontiguousarray(indices, dtype=np.uint32))
+    spec = flat_texture(tex_size, (0, 0, 0))
+    spec[:, ::8] = flat_texture(1, (200, 180, 160))[0, 0]
+    mesh.textures = [checker_texture(tex_size, 8), bump_normal_texture(tex_size), spec,
+                     flat_texture(tex_size, (200, 200, 200))]
+    cam = perspective_camera((0.0, 0.0, 3.0), 60.0, width, height)
+    return Scene("obj_sphere", width, height, bin_size, bin_size, cam, [mesh], cull=CULL_BACKFACE,
+                 sample=sample, vis=vis)
+
+
 def soup_vertices(n: int, width: int, height: int, seed: int = 0, blob_frac: float = 0.2,
                   blob_sigma: float = 100.0, area_min: float = 0.5, area_max: float = 4096.0) -> np.ndarray:
     """Triangle soup in NDC with w == 1: centroids uniform over the screen plus

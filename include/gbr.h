@@ -124,6 +124,32 @@ gbr_status gbr_texture_upload(gbr_renderer *r, const uint32_t *rgba8, uint32_t w
 /* CUDATextureManager::RemoveCUDATexture (CUDATextureManager.cpp:39-54) */
 gbr_status gbr_texture_remove(gbr_renderer *r, int32_t tex_id);
 
+/* ObjParser (ObjParser.h:8-48, ObjParser.cpp): Wavefront OBJ text ->
+ * IVertex vertices (GBR_VERTEX_IVERTEX56) + triangle-list indices, with the
+ * reference's line grammar, vertex de-duplication and tangent generation
+ * (gbr_obj.cpp states where it sets what the reference leaves unset).  A
+ * host-side reader: no device work. */
+typedef struct gbr_ivertex {
+    float p[3], uv[2], n[3], tan[3], c[3]; /* IVertex (Vertex.h:113-145), 56 B */
+} gbr_ivertex;
+/* VertexType (VertexType.h:3-11) flags of a read mesh */
+enum { GBR_VT_POS = 0, GBR_VT_UV = 1, GBR_VT_COL = 2, GBR_VT_NORM = 4, GBR_VT_TAN = 8, GBR_VT_VD = 16 };
+typedef struct gbr_obj_mesh {
+    gbr_ivertex *vertices;  /* num_vertices, malloc'd: release with gbr_obj_free */
+    uint32_t *indices;      /* num_indices (3 per face) */
+    uint32_t num_vertices, num_indices;
+    uint32_t num_faces;     /* "f" lines read */
+    int32_t vertex_type;    /* GBR_VT_* */
+} gbr_obj_mesh;
+/* ReadFromObjFile after OpenFile + SetInvertYAxis: `path` must end in the
+ * reference's ".obj" (from its first '.'); GBR_ERR_NOT_FOUND if it cannot be
+ * opened, GBR_ERR_INVALID_ARG (with the line) where the reference would throw
+ * or index out of range. */
+gbr_status gbr_obj_read_file(const char *path, int invert_y, gbr_obj_mesh *out);
+/* The same from text in memory. */
+gbr_status gbr_obj_read_text(const char *text, size_t length, int invert_y, gbr_obj_mesh *out);
+void gbr_obj_free(gbr_obj_mesh *mesh);
+
 /* Learned bin capacity (no counterpart in the reference, whose queues have a
  * fixed size and drop triangles when full, CUDAAtomicQueue.cuh:8-26).
  * gbr_set_predictor installs the capacity model: num_params BF16 parameters

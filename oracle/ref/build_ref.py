@@ -194,6 +194,28 @@ def build_erenderer(force: bool = False) -> str:
     return EREF_BIN
 
 
+OBJ_BIN = os.path.join(OUT, "obj_harness")
+
+
+def build_objparser(force: bool = False) -> str:
+    """Compile oracle/ref/obj_harness.cpp with the reference's ObjParser.cpp
+    (staged, unpatched) into oracle/_ref/obj_harness, with g++ at -O2 and no
+    floating-point contraction."""
+    if not os.path.isdir(SRC):
+        stage()
+    inputs = [os.path.join(HERE, "obj_harness.cpp"), os.path.join(SRC, ".staged")]
+    if not force and os.path.exists(OBJ_BIN) and all(os.path.getmtime(OBJ_BIN) >= os.path.getmtime(i) for i in inputs):
+        return OBJ_BIN
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    inc = ["-I", SRC, "-I", os.path.join(SRC, "sdl", "sdl2-2.0.9"), "-I", os.path.join(SRC, "sdl", "sdl2_image-2.0.5"),
+           "-I", cuda_inc]
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-w", "-ffp-contract=off", "-include", "cstring", *inc,
+           os.path.join(HERE, "obj_harness.cpp"), os.path.join(SRC, "ObjParser.cpp"), "-o", OBJ_BIN + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(OBJ_BIN + ".tmp", OBJ_BIN)
+    return OBJ_BIN
+
+
 if __name__ == "__main__":
     if "--stage" in sys.argv or os.path.isdir(CCR):
         stage(force="--force" in sys.argv)

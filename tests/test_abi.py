@@ -14,7 +14,7 @@ HEADER = os.path.join(ROOT, "include", "gbr.h")
 
 def declared_symbols():
     text = open(HEADER).read()
-    decl = r"^(?:gbr_status|const char \*|uint32_t)\s*\*?\s*(gbr_[a-z_]+)\s*\("
+    decl = r"^(?:gbr_status|const char \*|uint32_t|void)\s*\*?\s*(gbr_[a-z_]+)\s*\("
     return sorted(set(re.findall(decl, text, flags=re.M)))
 
 
