@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgbr.so")
-SOURCES = ["gbr_kernels.cu", "gbr_scan.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_predict.cu", "gbr_obj.cpp"]
+SOURCES = ["gbr_kernels.cu", "gbr_scan.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_predict.cu", "gbr_draw.cu", "gbr_obj.cpp"]
 HEADERS = ["gbr_device.cuh", "gbr_shade.cuh", "gbr_kernels.h", "gbr_predict.h", "gbr_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -403,7 +403,7 @@ gbr_status gbr_destroy(gbr_renderer* r) {
     if (r->in_batches) return fail(GBR_ERR_INVALID_ARG, "the renderer is in %u batch(es): destroy them first", r->in_batches);
     cudaDeviceSynchronize();
     gbr_scene_clear(r);
-    for (TexHost& t : r->textures) cudaFree(t.d_px);
+    for (TexHost& t : r->textures) free_texture(t);
     free_bins(r);
     cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis);
     cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_walk); cudaFree(r->d_keys); cudaFree(r->d_meshes); cudaFree(r->d_ctl); cudaFree(r->d_mlp_w);
@@ -578,8 +578,7 @@ gbr_status gbr_texture_remove(gbr_renderer* r, int32_t tex_id) {
     if (!r || tex_id < 0 || (size_t)tex_id >= r->textures.size() || !r->textures[tex_id].d_px)
         return fail(GBR_ERR_NOT_FOUND, "texture %d does not exist", tex_id);
     cudaDeviceSynchronize();
-    cudaFree(r->textures[tex_id].d_px);
-    r->textures[tex_id] = TexHost();
+    free_texture(r->textures[tex_id]);
     r->last_uploaded.clear();
     return GBR_OK;
 }
@@ -634,10 +633,12 @@ gbr_status gbr_render(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, uin
 
 gbr_status gbr_readback(gbr_renderer* r, uint32_t* colour, float* depth, void* stream) {
     if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
-    if (!r->have_frame) return fail(GBR_ERR_INVALID_ARG, "no frame rendered");
+    if (!r->have_frame && !r->drawn) return fail(GBR_ERR_INVALID_ARG, "no frame rendered");
     cudaStream_t s = (cudaStream_t)stream;
-    gbr_status st = finish_frame(r, s);
-    if (st != GBR_OK) return st;
+    if (r->have_frame) {
+        gbr_status st = finish_frame(r, s);
+        if (st != GBR_OK) return st;
+    }
     const size_t npx = (size_t)r->W * r->H;
     if (colour) GBR_CUDA(cudaMemcpyAsync(colour, r->d_colour, npx * 4u, cudaMemcpyDeviceToHost, s));
     if (depth) GBR_CUDA(cudaMemcpyAsync(depth, r->d_depth, npx * 4u, cudaMemcpyDeviceToHost, s));

@@ -35,7 +35,13 @@ struct MeshHost {
 struct TexHost {
     uint32_t* d_px = nullptr;
     uint32_t w = 0, h = 0;
+    // hardware texture object for gbr_draw_texture (made on first use, over
+    // a pitched copy when the rows are not aligned for a pitch-2D texture)
+    unsigned long long tex_obj = 0;
+    uint32_t* d_pitched = nullptr;
 };
+// Releases a texture's device memory and texture object (the device is idle).
+void free_texture(TexHost& t);
 
 // Matrix<4,4>::operator*(Matrix<4,4>) (Matrix4.h:120-143) on the host, left
 // to right with no fused multiply-add (built with -ffp-contract=off), as the
@@ -106,6 +112,7 @@ struct gbr_renderer {
     uint32_t num_lights = 0;
 
     bool have_frame = false;
+    bool drawn = false;   // a texture was drawn into the colour buffer (gbr_draw_texture*)
     gbr_camera last_cam{};
     uint32_t last_cull = 0, last_sample = 0, last_vis = 0;
     uint32_t overflow_reruns = 0;

@@ -37,7 +37,7 @@ EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "g
             "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
             "gbr_batch_set_view", "gbr_batch_set_config", "gbr_batch_get_config", "gbr_batch_autotune",
             "gbr_batch_set_timing", "gbr_batch_render", "gbr_batch_get_stats", "gbr_batch_scene_bins",
-            "gbr_batch_readback", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_obj_read_file", "gbr_obj_read_text",
+            "gbr_batch_readback", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_draw_texture", "gbr_draw_texture_global", "gbr_obj_read_file", "gbr_obj_read_text",
             "gbr_obj_free", "gbr_last_error_string", "gbr_version"]
 
 
@@ -138,6 +138,8 @@ def lib():
             "gbr_batch_scene_bins": [vp, u32, C.POINTER(u32), C.POINTER(u32)],
             "gbr_batch_readback": [vp, u32, vp, vp, vp, vp],
             "gbr_batch_get_bins": [vp, u32, vp, vp, u64, C.POINTER(u64), vp],
+            "gbr_draw_texture": [vp, C.c_int32, vp],
+            "gbr_draw_texture_global": [vp, C.c_int32, C.c_int, u32, vp],
             "gbr_obj_read_file": [C.c_char_p, C.c_int, C.POINTER(ObjMesh)],
             "gbr_obj_read_text": [C.c_char_p, C.c_size_t, C.c_int, C.POINTER(ObjMesh)],
         }
@@ -324,6 +326,16 @@ class Renderer:
                                      C.c_void_p(stream) if stream else None))
         c = colour.reshape(self.height, self.width)
         return (c, depth.reshape(self.height, self.width)) if want_depth else (c, None)
+
+    def draw_texture(self, tex_id: int, stream: int = 0):
+        """DrawTexture: the texture stretched over the colour buffer through
+        the texture hardware (readback() returns it)."""
+        check(self._lib.gbr_draw_texture(self.h, tex_id, _stream(stream)))
+
+    def draw_texture_global(self, tex_id: int, stretch_to_window: bool = True, sample: int = 0, stream: int = 0):
+        """DrawTextureGlobal: the shader's sampler over the colour buffer."""
+        check(self._lib.gbr_draw_texture_global(self.h, tex_id, 1 if stretch_to_window else 0, sample,
+                                                _stream(stream)))
 
     def readback_ids(self, stream: int = 0) -> np.ndarray:
         ids = np.empty(self.width * self.height, np.uint32)

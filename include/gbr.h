@@ -124,6 +124,19 @@ gbr_status gbr_texture_upload(gbr_renderer *r, const uint32_t *rgba8, uint32_t w
 /* CUDATextureManager::RemoveCUDATexture (CUDATextureManager.cpp:39-54) */
 gbr_status gbr_texture_remove(gbr_renderer *r, int32_t tex_id);
 
+/* DrawTexture (CUDARenderer.cu:1968-1988, TextureTestKernel :1565-1588):
+ * texture `tex_id` (gbr_texture_upload) stretched over the colour buffer
+ * through the texture hardware (normalised coordinates, point filtering,
+ * wrap addressing, as CUDATexture::Create sets it up), red and blue bytes
+ * swapped.  Asynchronous on `stream`; gbr_readback returns the image. */
+gbr_status gbr_draw_texture(gbr_renderer *r, int32_t tex_id, void *stream);
+/* DrawTextureGlobal (CUDARenderer.cu:1990-2012, DrawTextureGlobalKernel
+ * :1590-1615): uv = pixel / window size (stretch_to_window) or / texture
+ * size, the shader's sampler `sample` (GBR_SAMPLE_*), colour32 as the pixel
+ * shader writes it. */
+gbr_status gbr_draw_texture_global(gbr_renderer *r, int32_t tex_id, int stretch_to_window, uint32_t sample,
+                                   void *stream);
+
 /* ObjParser (ObjParser.h:8-48, ObjParser.cpp): Wavefront OBJ text ->
  * IVertex vertices (GBR_VERTEX_IVERTEX56) + triangle-list indices, with the
  * reference's line grammar, vertex de-duplication and tangent generation
