@@ -366,7 +366,7 @@ def run_ours(args, rank, world, local):
                              "peak_source": peak_kind, "algorithmic_bytes_per_launch": raster_bytes},
                 "e2e": {"value": world * N_TRI / t_e2e, "unit": UNIT, "h2d_bytes_per_step": vbytes,
                         "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
-                "gpu_launches": 7 * args.steps,   # setup, scan x3, fill, raster, shade
+                "gpu_launches": 5 * args.steps,   # setup, scan, fill, raster, shade
                 "clocks": clocks,
                 "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
@@ -426,7 +426,7 @@ def run_icosphere(args, rank, world, local):
                                      "resolution": [3840, 2160], "best_bins": best,
                                      "bins_8x8": per_bins[8], "bins_16x16": per_bins[16],
                                      "l2": "256 MB write between timed frames"},
-                          "gpu_launches": 7 * args.steps * 2, "clocks": clocks}), flush=True)
+                          "gpu_launches": 5 * args.steps * 2, "clocks": clocks}), flush=True)
 
 
 BATCH_SCENES = 256
@@ -538,7 +538,7 @@ def run_batch(args, rank, world, local):
                            "l2": "256 MB write between timed frames"},
                 "e2e": {"value": world * n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "gpu_launches": 8 * args.steps,   # reset, setup, scan x3, fill, raster, shade
+                "gpu_launches": 6 * args.steps,   # reset, setup, scan, fill, raster, shade
                 "clocks": clocks}
         print(json.dumps(line), flush=True)
     b.close()
