@@ -132,12 +132,13 @@ uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_
 }
 
 void free_bins(gbr_renderer* r) {
-    cudaFree(r->d_counts); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
+    cudaFree(r->d_counts); cudaFree(r->d_sub_base); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
     cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_scan);
     r->d_scan = nullptr;
     cudaFree(r->d_feat); cudaFree(r->d_features_out);
     r->d_feat = nullptr;
     r->d_features_out = nullptr;
+    r->d_sub_base = nullptr;
     r->d_counts = r->d_offsets = r->d_cursors = r->d_capacity = r->d_bin_done = r->d_list = nullptr;
     r->d_items = nullptr;
     r->items_cap = 0;
@@ -267,7 +268,9 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.raster_ctas = r->raster_ctas;
     F.meshes = r->d_meshes;
     F.setup = r->d_setup; F.rects = r->d_rects; F.keys = r->d_keys;
-    F.counts = r->d_counts; F.offsets = r->d_offsets; F.cursors = r->d_cursors; F.capacity = r->d_capacity;
+    F.counts = r->d_counts; F.sub_base = r->d_sub_base; F.count_stride = nb; F.offsets = r->d_offsets;
+    F.cursors = r->d_cursors; F.capacity = r->d_capacity;
+    F.count_split = count_split_for(r->seen_pairs, nb);   // 1 until a frame has been seen
     F.bin_done = r->d_bin_done;
     F.items = r->d_items; F.items_cap = r->items_cap;
     F.list = r->d_list; F.list_cap = r->list_cap;
@@ -429,8 +432,9 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     free_bins(r);
     r->nbx = num_bins_x; r->nby = num_bins_y; r->bw = bin_w; r->bh = bin_h; r->chunk = queue_chunk;
     const uint32_t nb = num_bins_x * num_bins_y;
-    GBR_CUDA(cudaMalloc(&r->d_counts, nb * sizeof(uint32_t)));
-    GBR_CUDA(cudaMemset(r->d_counts, 0, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_counts, (size_t)kCountSplit * nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_counts, 0, (size_t)kCountSplit * nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_sub_base, (size_t)kCountSplit * nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_offsets, (nb + 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_offsets, 0, (nb + 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_cursors, nb * sizeof(uint32_t)));

@@ -65,7 +65,9 @@ struct gbr_batch {
 
     // device storage
     uint32_t* d_tables = nullptr;        // tri_blocks | px_blocks | bin_base, num_scenes + 1 each
-    uint32_t* d_counts = nullptr;
+    uint32_t* d_counts = nullptr;     // kCountSplit x bins
+    uint32_t* d_sub_base = nullptr;   // kCountSplit x bins
+    uint32_t count_split = 1;         // sub-counters per bin in use
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
     ScanState* d_scan = nullptr;   // bin scan state (zeroed once)
@@ -109,9 +111,10 @@ void drop_graph(gbr_batch* b) {
 }
 
 void free_layout_storage(gbr_batch* b) {
-    cudaFree(b->d_tables); cudaFree(b->d_counts); cudaFree(b->d_offsets); cudaFree(b->d_cursors);
+    cudaFree(b->d_tables); cudaFree(b->d_counts); cudaFree(b->d_sub_base); cudaFree(b->d_offsets); cudaFree(b->d_cursors);
     cudaFree(b->d_setup); cudaFree(b->d_rects); cudaFree(b->d_scan); cudaFree(b->d_walk); cudaFree(b->d_keys);
     b->d_tables = b->d_counts = b->d_offsets = b->d_cursors = nullptr;
+    b->d_sub_base = nullptr;
     b->d_scan = nullptr;
     b->d_setup = nullptr;
     b->d_rects = nullptr;
@@ -200,8 +203,9 @@ gbr_status ensure_layout(gbr_batch* b) {
 
     GBR_CUDA(cudaMalloc(&b->d_tables, tables.size() * sizeof(uint32_t)));
     GBR_CUDA(cudaMemcpy(b->d_tables, tables.data(), tables.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    GBR_CUDA(cudaMalloc(&b->d_counts, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
-    GBR_CUDA(cudaMemset(b->d_counts, 0, std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&b->d_counts, kCountSplit * std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(b->d_counts, 0, kCountSplit * std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&b->d_sub_base, kCountSplit * std::max<uint64_t>(bins, 1u) * sizeof(uint32_t)));
     // one scan over the bins of every scene: scene s's offsets are entries
     // [bin_base[s], bin_base[s+1]] of the batch-wide array
     GBR_CUDA(cudaMalloc(&b->d_offsets, (bins + 1u) * sizeof(uint32_t)));
@@ -262,6 +266,9 @@ void build_table(gbr_batch* b, std::vector<unsigned char>& out) {
         F.rects = b->d_rects + L.tri_base;
         F.keys = b->d_keys + L.tri_base;
         F.counts = b->d_counts + L.bin_base;
+        F.sub_base = b->d_sub_base + L.bin_base;
+        F.count_stride = b->total_bins;   // sub-counter rows span every scene's bins
+        F.count_split = b->count_split;
         F.offsets = b->d_offsets + L.bin_base;
         F.cursors = b->d_cursors + L.bin_base;
         F.list = b->d_list;
@@ -303,6 +310,8 @@ gbr_status capture_graph(gbr_batch* b) {
     const BatchDev B = batch_dev(b);
     memset(&L.scan, 0, sizeof L.scan);
     L.scan.counts = b->d_counts;
+    L.scan.sub_base = b->d_sub_base;
+    L.scan.split = b->count_split;
     L.scan.offsets = b->d_offsets;
     L.scan.cursors = b->d_cursors;
     L.scan.items = b->d_items;
@@ -376,6 +385,13 @@ gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
         GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     }
     if (b->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "batch bin storage overflow persists");
+    // sub-counters per bin for the next frames, from this frame's density
+    // (a change is captured anew: the scan's parameters live in the graph)
+    const uint32_t split = count_split_for(b->h_ctl->num_pairs, b->total_bins);
+    if (split != b->count_split) {
+        b->count_split = split;
+        drop_graph(b);
+    }
     if (b->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
         GBR_CUDA(cudaMemset(b->d_scan, 0, scan_state_bytes(b->total_bins)));
         return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the batch frame is invalid");

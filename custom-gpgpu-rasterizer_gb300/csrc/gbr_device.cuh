@@ -27,6 +27,16 @@ constexpr int kDepthBuckets = 256;                // front-to-back buckets: top 
 constexpr uint32_t kPhase = 16;                   // triangles between hierarchical-z refreshes
 constexpr uint32_t kMaxPhase = 64;                // setup records staged per phase
 constexpr uint32_t kMinChunk = 64;                // smallest raster work item the library picks
+// Exact binning counts each bin in `count_split` sub-counters (at most
+// kCountSplit), walk w using sub-counter w mod count_split: the crowded
+// bins' atomics (a thousand per bin across the 1M soup, several thousand at
+// its centre) queue on several addresses instead of one.  More sub-counters
+// cost the scan a read and a write each per bin, so sparse frames use one.
+constexpr uint32_t kCountSplit = 8;
+__host__ __device__ inline uint32_t count_split_for(unsigned long long pairs, uint32_t bins) {
+    const unsigned long long per_bin = pairs / (bins ? bins : 1u);
+    return per_bin >= 256u ? 8u : per_bin >= 64u ? 4u : per_bin >= 16u ? 2u : 1u;
+}
 constexpr uint32_t kDefaultRasterCtas = 6;        // raster_kernel variant (CTAs per SM) used by default
 
 enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
@@ -109,7 +119,8 @@ struct FrameDev {
     TriSetup* setup;
     uint2* rects;
     uint32_t* keys;            // per triangle: lower bound of its fragments' depth keys (hiz_key)
-    uint32_t* counts;
+    uint32_t* counts;          // kCountSplit sub-counters per bin: counts[k * count_stride + bin]
+    uint32_t* sub_base;        // first list entry of each sub-counter's pairs (same layout)
     uint32_t* offsets;        // num_bins + 1
     uint32_t* cursors;
     uint32_t* capacity;       // predicted per-bin capacity (predicted binning)
@@ -140,6 +151,8 @@ struct FrameDev {
     uint32_t* walk_base;       // first slot of each walk (walk = triangle slot / 32)
     uint32_t* rank_next;       // slot reservation counter (a Ctl's rank_next)
     unsigned long long rank_cap;
+    uint32_t count_stride;     // bins between sub-counter rows (the scan's bin count)
+    uint32_t count_split;      // sub-counters per bin in use: 1, 2, 4 or 8
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -174,7 +187,9 @@ __host__ __device__ constexpr size_t scan_state_bytes(uint32_t num_bins) {
 }
 
 struct ScanDev {
-    uint32_t* counts;              // exact counts, zeroed for the next frame
+    uint32_t* counts;              // exact sub-counts (kCountSplit rows of stride n), zeroed for the next frame
+    uint32_t* sub_base;            // exact modes: list start of each sub-count (same layout)
+    uint32_t split;                // sub-counters per bin in use
     const uint32_t* capacity;      // predicted capacities
     uint32_t* offsets;             // n + 1
     uint32_t* cursors;
@@ -431,16 +446,19 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
 // owner's rectangle.  A lane takes up to kPairsPerLane pairs per pass and
 // issues their atomics back to back: atomics with return are bound by their
 // latency, so several must be in flight per lane.
-// Mode 0: count (atomicAdd on counts; its return, the pair's rank within the
-// bin, is kept in the walk's rank slots), 1: fill (entry at the bin's offset
-// + rank: no atomics), 2: predicted fill (append within the bin's predicted
+// Mode 0: count (atomicAdd on the walk's sub-counter of the bin; its return,
+// the pair's rank there, is kept in the walk's rank slots), 1: fill (entry
+// at the sub-counter's list start + rank: no atomics), 2: predicted fill (append within the bin's predicted
 // capacity), 3: pre-pass count (atomicAdd on the first feature slot).  A
 // walk is identified by `walk` (its first triangle slot / 32), so the count
 // and fill passes of the same triangles meet the same slots.  One atomic per
 // pair: merging the atomics of same-bin lanes -- every such lane of the warp
 // (__match_any_sync) or runs of neighbouring lanes -- measured 8-10% slower
 // on GB300 for both the 1M soup and the 4K icosphere.
-constexpr uint32_t kPairsPerLane = 4;
+#ifndef GBR_PAIRS_PER_LANE
+#define GBR_PAIRS_PER_LANE 4
+#endif
+constexpr uint32_t kPairsPerLane = GBR_PAIRS_PER_LANE;
 
 template <int MODE>
 __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid, uint32_t walk) {
@@ -465,6 +483,7 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
     // exact binning: the walk's rank slots, reserved by the count pass and
     // found again by the fill pass (same triangles, same enumeration)
     uint32_t wb = 0;
+    const uint32_t krow = (walk & (F.count_split - 1u)) * F.count_stride;   // the walk's sub-counter row
     if (MODE == 0) {
         if (lane == 0) {
             wb = atomicAdd(F.rank_next, total);
@@ -511,20 +530,20 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
             // storage are dropped: that frame overflows and is not filled)
             uint32_t rank[kPairsPerLane];
 #pragma unroll
-            for (uint32_t u = 0; u < kPairsPerLane; ++u) rank[u] = act[u] ? atomicAdd(&F.counts[bin[u]], 1u) : 0u;
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) rank[u] = act[u] ? atomicAdd(&F.counts[krow + bin[u]], 1u) : 0u;
 #pragma unroll
             for (uint32_t u = 0; u < kPairsPerLane; ++u) {
                 const unsigned long long slot = (unsigned long long)wb + base + u * 32u + lane;
                 if (act[u] && slot < F.rank_cap) F.ranks[slot] = rank[u];
             }
         } else if (MODE == 1) {
-            // fill: the bin's offset plus the rank the count pass kept
+            // fill: the sub-counter's list start plus the rank the count pass kept
             uint32_t rank[kPairsPerLane];
 #pragma unroll
             for (uint32_t u = 0; u < kPairsPerLane; ++u) rank[u] = act[u] ? __ldg(&F.ranks[wb + base + u * 32u + lane]) : 0u;
 #pragma unroll
             for (uint32_t u = 0; u < kPairsPerLane; ++u)
-                if (act[u]) F.list[__ldg(&F.offsets[bin[u]]) + rank[u]] = ent[u];
+                if (act[u]) F.list[__ldg(&F.sub_base[krow + bin[u]]) + rank[u]] = ent[u];
         } else {
             uint32_t pos[kPairsPerLane];
 #pragma unroll

@@ -82,7 +82,8 @@ struct gbr_renderer {
     uint32_t* d_ids = nullptr;
     unsigned long long* d_gvis = nullptr;
 
-    uint32_t* d_counts = nullptr;
+    uint32_t* d_counts = nullptr;     // kCountSplit x bins
+    uint32_t* d_sub_base = nullptr;   // kCountSplit x bins
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
     uint32_t* d_capacity = nullptr;

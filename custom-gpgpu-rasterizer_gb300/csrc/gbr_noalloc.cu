@@ -47,7 +47,8 @@ constexpr size_t align256(size_t x) { return (x + 255u) & ~size_t(255u); }
 constexpr size_t kOffSetup = 0;
 constexpr size_t kOffRects = kOffSetup + align256(size_t(kNaMaxTris) * sizeof(TriSetup));
 constexpr size_t kOffCounts = kOffRects + align256(size_t(kNaMaxTris) * sizeof(uint2));
-constexpr size_t kOffOffsets = kOffCounts + align256(size_t(kNaMaxBins) * 4u);
+constexpr size_t kOffSubBase = kOffCounts + align256(size_t(kCountSplit) * kNaMaxBins * 4u);
+constexpr size_t kOffOffsets = kOffSubBase + align256(size_t(kCountSplit) * kNaMaxBins * 4u);
 constexpr size_t kOffCursors = kOffOffsets + align256(size_t(kNaMaxBins + 1u) * 4u);
 constexpr size_t kOffCapacity = kOffCursors + align256(size_t(kNaMaxBins) * 4u);
 constexpr size_t kOffBinDone = kOffCapacity + align256(size_t(kNaMaxBins) * 4u);
@@ -84,7 +85,8 @@ __global__ void noalloc_prepare_kernel(FrameDev F, MeshDev desc, uint32_t npx) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += stride) F.gvis[i] = kEmptyVis;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < F.num_bins; i += stride) {
-        F.counts[i] = 0u;
+#pragma unroll
+        for (uint32_t k = 0; k < kCountSplit; ++k) F.counts[k * F.num_bins + i] = 0u;
         F.bin_done[i] = 0u;
     }
     // the caller's scratch: the bin scan state starts zeroed every frame
@@ -175,6 +177,9 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.rects = reinterpret_cast<uint2*>(b + kOffRects);
     F.keys = reinterpret_cast<uint32_t*>(b + kOffKeys);
     F.counts = reinterpret_cast<uint32_t*>(b + kOffCounts);
+    F.sub_base = reinterpret_cast<uint32_t*>(b + kOffSubBase);
+    F.count_stride = F.num_bins;
+    F.count_split = 1u;   // no frame history: one counter per bin
     F.offsets = reinterpret_cast<uint32_t*>(b + kOffOffsets);
     F.cursors = reinterpret_cast<uint32_t*>(b + kOffCursors);
     F.capacity = reinterpret_cast<uint32_t*>(b + kOffCapacity);

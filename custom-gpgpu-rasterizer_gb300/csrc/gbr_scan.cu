@@ -29,12 +29,9 @@ __device__ __forceinline__ bool scan_runs(const ScanDev& S) {
     return S.mode != kScanExactAfterPredicted || S.ctl->pred_overflow != 0u;
 }
 
-__device__ __forceinline__ uint32_t bin_size(const ScanDev& S, uint32_t b) {
-    switch (S.mode) {
-        case kScanCapacity: return S.capacity[b];
-        case kScanPredictedItems: return min(S.cursors[b] - S.offsets[b], S.capacity[b]);
-        default: return S.counts[b];
-    }
+// Entries of bin b in the predicted modes (capacity, or filled within it).
+__device__ __forceinline__ uint32_t predicted_size(const ScanDev& S, uint32_t b) {
+    return S.mode == kScanCapacity ? S.capacity[b] : min(S.cursors[b] - S.offsets[b], S.capacity[b]);
 }
 
 // Raster work items of a bin of c entries (an empty bin has none: its pixels
@@ -185,10 +182,22 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
     const uint32_t b = tile * 1024u + threadIdx.x;
     const bool exact = S.mode == kScanExact || S.mode == kScanExactAfterPredicted;
     uint32_t c = 0, it = 0;
+    uint32_t sub[kCountSplit];   // exact modes: the bin's sub-counts (zeroed for the next frame)
     if (b < S.n) {
-        c = bin_size(S, b);
+        if (exact) {
+#pragma unroll
+            for (uint32_t k = 0; k < kCountSplit; ++k) {
+                sub[k] = 0u;
+                if (k < S.split) {
+                    sub[k] = S.counts[k * S.n + b];
+                    S.counts[k * S.n + b] = 0u;
+                    c += sub[k];
+                }
+            }
+        } else {
+            c = predicted_size(S, b);
+        }
         it = bin_items(c, S.chunk);
-        if (exact) S.counts[b] = 0u;   // zeroed for the next frame
     }
     unsigned long long ia = c, ib = it, ta, tb;
     block_scan2(ia, ib, s_a, s_b, ta, tb);
@@ -217,7 +226,12 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
         } else {
             if (exact) {
                 S.offsets[b] = (uint32_t)run;
-                S.cursors[b] = (uint32_t)run;
+                uint32_t at = (uint32_t)run;   // each sub-counter's pairs follow the previous one's
+#pragma unroll
+                for (uint32_t k = 0; k < kCountSplit; ++k) {
+                    if (k < S.split) S.sub_base[k * S.n + b] = at;
+                    at += sub[k];
+                }
             }
             if (item + it <= S.items_cap) {
                 const uint32_t start = exact ? (uint32_t)run : S.offsets[b];
@@ -253,6 +267,8 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
 ScanDev scan_of(const FrameDev& F, uint32_t mode) {
     ScanDev S;
     S.counts = F.counts;
+    S.sub_base = F.sub_base;
+    S.split = F.count_split;
     S.capacity = F.capacity;
     S.offsets = F.offsets;
     S.cursors = F.cursors;

@@ -87,10 +87,16 @@ def test_batch_equals_single_frames(gbr_lib, cuda_device, bin_size, chunk):
     assert st["num_scenes"] == len(sl) and st["graph_captures"] >= 1
     assert st["num_triangles"] == sum(s.num_triangles for s in sl)
     assert_batch_equals_single(gbr_lib, b, sl, bin_size, chunk)
-    # a second frame replays the captured graph
+    # the second frame may capture once more (the sub-counters per bin follow
+    # the first frame's density); it renders the same bins, and later frames
+    # replay the captured graph
     b.render()
     st2 = b.stats()
-    assert st2["graph_captures"] == st["graph_captures"] and st2["num_pairs"] == st["num_pairs"]
+    assert st2["graph_captures"] <= st["graph_captures"] + 1 and st2["num_pairs"] == st["num_pairs"]
+    assert_batch_equals_single(gbr_lib, b, sl, bin_size, chunk)
+    b.render()
+    st3 = b.stats()
+    assert st3["graph_captures"] == st2["graph_captures"] and st3["num_pairs"] == st["num_pairs"]
     close_batch(b, rs)
 
 
