@@ -13,6 +13,18 @@
 
 namespace gbr {
 
+// b / 255 for every byte value b, each the correctly rounded quotient
+// (evaluated at compile time in single precision): the RGBA8 vertex colours
+// read as GetRGBColor (RGBRaw.h:34-38) divides, without a division per use
+// (a product with 1/255 differs in 126 of the 256 values).
+struct ByteOver255 {
+    float v[256];
+    constexpr ByteOver255() : v() {
+        for (int b = 0; b < 256; ++b) v[b] = (float)b / 255.0f;
+    }
+};
+__device__ constexpr ByteOver255 kByteOver255{};
+
 struct OVtx {
     float px, py, pz, pw;  // NDC xyz, clip w
     float u, v;
@@ -28,9 +40,9 @@ __device__ __forceinline__ void fetch_full(const MeshDev& m, uint32_t vi, float 
 #pragma unroll
         for (int k = 3; k < 11; ++k) iv[k] = 0.f;
         // GetRGBColor (RGBRaw.h:34-38): r = byte0 / 255
-        iv[11] = __fdiv_rn((float)(rgba & 0xFFu), 255.f);
-        iv[12] = __fdiv_rn((float)((rgba >> 8) & 0xFFu), 255.f);
-        iv[13] = __fdiv_rn((float)((rgba >> 16) & 0xFFu), 255.f);
+        iv[11] = kByteOver255.v[rgba & 0xFFu];
+        iv[12] = kByteOver255.v[(rgba >> 8) & 0xFFu];
+        iv[13] = kByteOver255.v[(rgba >> 16) & 0xFFu];
     } else {
         const float2* b = reinterpret_cast<const float2*>(reinterpret_cast<const float*>(m.vertices) + 14u * (size_t)vi);
 #pragma unroll
@@ -62,9 +74,8 @@ __device__ __forceinline__ OVtx vertex_stage(const MeshDev& m, const FrameDev& F
     return o;
 }
 
-__device__ __forceinline__ F3 rgb_of(uint32_t c) {
-    return f3(__fdiv_rn((float)(c & 0xFFu), 255.f), __fdiv_rn((float)((c >> 8) & 0xFFu), 255.f),
-              __fdiv_rn((float)((c >> 16) & 0xFFu), 255.f));
+__device__ __forceinline__ F3 rgb_of(uint32_t c) {   // byte / 255 per channel
+    return f3(kByteOver255.v[c & 0xFFu], kByteOver255.v[(c >> 8) & 0xFFu], kByteOver255.v[(c >> 16) & 0xFFu]);
 }
 
 // SamplePoint (CUDATextureSampler.cuh:87-104): u = int(uv.x*w + 0.5);
