@@ -222,8 +222,10 @@ struct RasterShared {
     __align__(16) FrameDev frame;
 };
 
+// `key_bound` = hiz_key(t): a covered pixel whose stored key is already
+// below it cannot be won by this triangle, and skips the weights and depth.
 __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
-                                             int ty0, int tw, int th, uint32_t lane) {
+                                             int ty0, int tw, int th, uint32_t lane, uint32_t key_bound) {
     const int X0 = snap_fx(t.x0), Y0 = snap_fx(t.y0), X1 = snap_fx(t.x1);
     const int Y1 = snap_fx(t.y1), X2 = snap_fx(t.x2), Y2 = snap_fx(t.y2);
     const int minx = min(X0, min(X1, X2)), maxx = max(X0, max(X1, X2));
@@ -254,6 +256,9 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
         for (int sx = px0; sx <= px1; sx += sw, e2 += ix2, e0 += ix0, e1 += ix1) {
             const int x = sx + lx;
             if (x > px1 || y > py1 || (e0 | e1 | e2) < 0) continue;
+            unsigned long long* slot = tile + (y - ty0) * tw + (x - tx0);
+            const unsigned long long cur = *((volatile unsigned long long*)slot);
+            if ((uint32_t)(cur >> 32) < key_bound) continue;   // occluded: every fragment key is >= the bound
             float w[3];
             weights_fixed(t, x, y, w);
             const float z = interp_z(w[0], w[1], w[2], t.z0, t.z1, t.z2);
@@ -262,8 +267,7 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
             if (!(z >= 0.f && z < 1.f)) continue;
             const uint32_t key = (uint32_t)__float2int_rz(__fmul_rn(z, 2147483648.0f));
             const unsigned long long packed = ((unsigned long long)key << 32) | prim;
-            unsigned long long* slot = tile + (y - ty0) * tw + (x - tx0);
-            if (packed < *((volatile unsigned long long*)slot)) atomicMin(slot, packed);
+            if (packed < cur) atomicMin(slot, packed);   // a later, lower value only makes atomicMin a no-op
         }
     }
 }
@@ -492,7 +496,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                     if (S.key[i] > tile_max) continue;
                     const TriSetup& t = S.rec[(uint32_t)k & (kMaxPhase - 1u)];
                     if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
-                    else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
+                    else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane, S.key[i]);
                 }
             }
         }
