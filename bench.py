@@ -59,6 +59,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(values, dist, device):
+    """Element-wise maximum of `values` over the ranks (a replica job takes
+    as long as its slowest rank); unchanged with one rank."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
 def make_scene(seed: int):
     import scenes
     return scenes.soup_scene(N_TRI, WIDTH, HEIGHT, BIN, seed=seed)
@@ -295,10 +306,7 @@ def run_ours(args, rank, world, local):
     predicted = predicted_binning(r, scene, args, stream, flush)
     pairs = st["num_pairs"]
     t_frame = sum(ms_total) / len(ms_total) / 1e3
-    if dist:
-        tt = torch.tensor([t_frame], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_frame = float(tt.item())
+    (t_frame,) = max_over_ranks([t_frame], dist, dev)
     value = world * N_TRI / t_frame
     t_raster = sum(ms_raster) / len(ms_raster) / 1e3
     raster_bytes = 4 * pairs + 8 * WIDTH * HEIGHT
@@ -345,10 +353,7 @@ def run_ours(args, rank, world, local):
     e2e_steps(args.steps)
     torch.cuda.synchronize(dev)
     t_e2e = (time.perf_counter() - t0) / args.steps
-    if dist:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    (t_e2e,) = max_over_ranks([t_e2e], dist, dev)
     for rr in rs:
         rr.close()
 
@@ -535,10 +540,7 @@ def run_batch(args, rank, world, local):
             if step >= args.warmup:
                 e2e.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e)
-    if dist:
-        tt = torch.tensor([t_batch, t_e2e, t_seq], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_batch, t_e2e, t_seq = (float(x) for x in tt.tolist())
+    t_batch, t_e2e, t_seq = max_over_ranks([t_batch, t_e2e, t_seq], dist, dev)
     line = None
     if rank == 0:
         line = {"metric": BATCH_METRIC, "value": world * n_tri / t_batch, "unit": UNIT, "n_gpus": world,
