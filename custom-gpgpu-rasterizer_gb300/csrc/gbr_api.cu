@@ -650,6 +650,17 @@ gbr_status gbr_readback(gbr_renderer* r, uint32_t* colour, float* depth, void* s
     return GBR_OK;
 }
 
+gbr_status gbr_predicted_capacities(gbr_renderer* r, uint32_t* capacities, void* stream) {
+    if (!r || !capacities) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    if (!r->have_frame || !r->last_predicted) return fail(GBR_ERR_INVALID_ARG, "no predicted-binning frame rendered");
+    cudaStream_t s = (cudaStream_t)stream;
+    gbr_status st = finish_frame(r, s);
+    if (st != GBR_OK) return st;
+    GBR_CUDA(cudaMemcpyAsync(capacities, r->d_capacity, (size_t)r->nbx * r->nby * 4u, cudaMemcpyDeviceToHost, s));
+    GBR_CUDA(cudaStreamSynchronize(s));
+    return GBR_OK;
+}
+
 gbr_status gbr_readback_ids(gbr_renderer* r, uint32_t* ids, void* stream) {
     if (!r || !ids) return fail(GBR_ERR_INVALID_ARG, "null argument");
     if (!r->have_frame) return fail(GBR_ERR_INVALID_ARG, "no frame rendered");

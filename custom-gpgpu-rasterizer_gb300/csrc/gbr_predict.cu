@@ -273,6 +273,203 @@ __global__ void __launch_bounds__(256) capacity_kernel(FrameDev F, int predict) 
 }
 
 // ---------------------------------------------------------------------------
+// Capacity inference on the tensor cores (tcgen05, accumulators in TMEM)
+// ---------------------------------------------------------------------------
+// One CTA of 128 threads takes 128 bins: thread t computes bin t's
+// features into row t of the layer-1 operand.  Layer 1 is one
+// tcgen05.mma (M 128, N 64, K 16: the 12 features padded with zeros),
+// layer 2 four (K 64), each BF16 x BF16 with FP32 accumulation into tensor
+// memory (columns 0-63 and 64-127 of a 128-column allocation).  Thread t
+// reads row t back (TMEM lane t: warp w owns lanes 32w..32w+31), adds the
+// bias and applies ReLU in FP32; the hidden layer is rounded to BF16 as the
+// next MMA's operand; the 64 -> 1 output layer, softplus and the capacity
+// rule run in FP32 registers.  Operands sit in shared memory in the
+// canonical no-swizzle K-major layout: 8 x 8 core matrices of 16-byte rows,
+// consecutive in K (leading offset 128 B), then in M / N (stride offset
+// K / 8 x 128 B).  The two waits on the MMAs' mbarrier are bounded: one
+// that gives up flags Ctl::error and leaves the CTA's bins at the triangle
+// count.
+namespace tc {
+
+constexpr uint32_t kM = 128, kN = 64, kK1 = 16, kK2 = 64;
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (row, k) of a K-major tile with `kdim` columns
+__device__ __forceinline__ uint32_t kmajor_offset(uint32_t row, uint32_t k, uint32_t kdim) {
+    return (row >> 3) * (kdim / 8u) * 128u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// shared-memory matrix descriptor: start, leading and stride byte offsets
+// (all >> 4), descriptor version 1, no swizzle
+__device__ __forceinline__ unsigned long long smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (unsigned long long)((addr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both
+// K-major, N and M
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t m, uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, unsigned long long a, unsigned long long b, uint32_t idesc,
+                                    uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+// waits for phase `parity` of the mbarrier; false when the bound ran out
+__device__ __forceinline__ bool wait(uint32_t mbar, uint32_t parity) {
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ uint16_t bf16_bits(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(128) capacity_tc_kernel(FrameDev F) {
+    using namespace tc;
+    __shared__ __align__(128) unsigned char sA1[kM * kK1 * 2];   // features (bf16)
+    __shared__ __align__(128) unsigned char sB1[kN * kK1 * 2];   // W1^T
+    __shared__ __align__(128) unsigned char sA2[kM * kK2 * 2];   // hidden layer (bf16)
+    __shared__ __align__(128) unsigned char sB2[kN * kK2 * 2];   // W2^T
+    __shared__ float sb1[kN], sb2[kN], sw3[kN];
+    __shared__ __align__(8) unsigned long long s_mbar;
+    __shared__ uint32_t s_tmem;
+    pdl_wait();
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint16_t* w = F.mlp_w;
+    // W1^T (n = hidden unit, k = feature, zero past feature 11) and W2^T
+    for (uint32_t i = tid; i < kN * kK1; i += blockDim.x) {
+        const uint32_t n = i / kK1, k = i % kK1;
+        const uint16_t v = k < (uint32_t)kFeatures ? w[kOffW1 + k * kMlpHidden + n] : (uint16_t)0;
+        *reinterpret_cast<uint16_t*>(sB1 + kmajor_offset(n, k, kK1)) = v;
+    }
+    for (uint32_t i = tid; i < kN * kK2; i += blockDim.x) {
+        const uint32_t n = i / kK2, k = i % kK2;
+        *reinterpret_cast<uint16_t*>(sB2 + kmajor_offset(n, k, kK2)) = w[kOffW2 + k * kMlpHidden + n];
+    }
+    if (tid < kN) {
+        sb1[tid] = bf16_to_f32(w[kOffB1 + tid]);
+        sb2[tid] = bf16_to_f32(w[kOffB2 + tid]);
+        sw3[tid] = bf16_to_f32(w[kOffW3 + tid]);
+    }
+    // this thread's bin: its features as row `tid` of the layer-1 operand
+    const uint32_t b = blockIdx.x * kM + tid;
+    float x[kFeatures];
+#pragma unroll
+    for (int k = 0; k < kFeatures; ++k) x[k] = 0.f;
+    if (b < F.num_bins) bin_features(F, b, x);
+#pragma unroll
+    for (uint32_t k = 0; k < kK1; ++k)
+        *reinterpret_cast<uint16_t*>(sA1 + kmajor_offset(tid, k, kK1)) = k < (uint32_t)kFeatures ? bf16_bits(x[k]) : 0;
+    const uint32_t mbar = smem_u32(&s_mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&s_tmem))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();   // the operands written above, to the tensor cores' (async) proxy
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = s_tmem;
+    constexpr uint32_t idesc = instr_desc(kM, kN);
+    if (tid == 0) {
+        mma(tmem, smem_desc(smem_u32(sA1), 128u, (kK1 / 8u) * 128u), smem_desc(smem_u32(sB1), 128u, (kK1 / 8u) * 128u),
+            idesc, 0u);
+        commit(mbar);
+    }
+    bool ok = wait(mbar, 0u);
+    fence_after();
+    const uint32_t lane_base = (warp * 32u) << 16;   // TMEM lane field
+    uint32_t r[16];
+    if (ok) {
+#pragma unroll
+        for (uint32_t c = 0; c < kN; c += 16) {
+            ld16(tmem + lane_base + c, r);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (uint32_t j = 0; j < 16; ++j) {
+                const float h = fmaxf(__uint_as_float(r[j]) + sb1[c + j], 0.f);
+                *reinterpret_cast<uint16_t*>(sA2 + kmajor_offset(tid, c + j, kK2)) = bf16_bits(h);
+            }
+        }
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    ok = __syncthreads_and(ok ? 1 : 0) != 0;   // every thread saw layer 1 arrive
+    if (ok && tid == 0) {
+#pragma unroll
+        for (uint32_t s = 0; s < kK2 / 16u; ++s)
+            mma(tmem + kN, smem_desc(smem_u32(sA2) + s * 256u, 128u, (kK2 / 8u) * 128u),
+                smem_desc(smem_u32(sB2) + s * 256u, 128u, (kK2 / 8u) * 128u), idesc, s > 0 ? 1u : 0u);
+        commit(mbar);
+    }
+    if (ok) ok = wait(mbar, 1u);
+    fence_after();
+    float y = bf16_to_f32(w[kOffB3]);
+    if (ok) {
+#pragma unroll
+        for (uint32_t c = 0; c < kN; c += 16) {
+            ld16(tmem + lane_base + kN + c, r);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (uint32_t j = 0; j < 16; ++j) y = __fmaf_rn(fmaxf(__uint_as_float(r[j]) + sb2[c + j], 0.f), sw3[c + j], y);
+        }
+    }
+    if (b < F.num_bins) {
+        const float most = (float)F.num_tris;
+        float cap = most;   // a bin the model could not score gets the bound
+        if (ok) {
+            const float l = softplus(y);
+            const float c = ceilf(l * (1.f + F.cap_alpha) + F.cap_beta * sqrtf(l + 1.f) + F.cap_gamma);
+            cap = c == c ? fminf(fmaxf(c, 0.f), most) : most;
+        }
+        F.capacity[b] = (uint32_t)cap;
+    }
+    if (!ok && tid == 0) atomicOr(&F.ctl->error, 2u);
+    fence_before();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Training kernels
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) mlp_predict_kernel(const uint16_t* wq, const float* x, uint32_t n, float* out) {
@@ -409,10 +606,11 @@ cudaError_t launch_prepass(const FrameDev& F, cudaStream_t s) {
 }
 
 cudaError_t launch_capacity(const FrameDev& F, bool predict, cudaStream_t s) {
-    // 8 warps per block, one bin per warp up to 4096 blocks (then a few)
+    if (predict)   // the model on the tensor cores, 128 bins per CTA
+        return launch_pdl(capacity_tc_kernel, dim3(std::max<uint32_t>((F.num_bins + 127u) / 128u, 1u)), dim3(128), 0, s, F);
+    // features only (training data): 8 warps per block, one bin per warp
     const uint32_t blocks = std::min<uint32_t>((F.num_bins + 7u) / 8u, 4096u);
-    return launch_pdl(capacity_kernel, dim3(blocks ? blocks : 1u), dim3(256), 0, s, F, predict ? 1 : 0);
-    return cudaGetLastError();
+    return launch_pdl(capacity_kernel, dim3(blocks ? blocks : 1u), dim3(256), 0, s, F, 0);
 }
 
 

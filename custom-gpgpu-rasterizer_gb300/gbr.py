@@ -32,7 +32,7 @@ TIMING_OFF, TIMING_STAGES, TIMING_TOTAL = 0, 1, 2
 EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "gbr_mesh_update_vertices",
             "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
             "gbr_texture_upload", "gbr_texture_remove", "gbr_set_lights", "gbr_set_binning", "gbr_set_predictor",
-            "gbr_collect_bin_features", "gbr_mlp_num_params", "gbr_mlp_predict", "gbr_mlp_loss_grad", "gbr_mlp_adam",
+            "gbr_collect_bin_features", "gbr_predicted_capacities", "gbr_mlp_num_params", "gbr_mlp_predict", "gbr_mlp_loss_grad", "gbr_mlp_adam",
             "gbr_set_raster_params", "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
             "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
             "gbr_batch_set_view", "gbr_batch_set_config", "gbr_batch_get_config", "gbr_batch_autotune",
@@ -112,6 +112,7 @@ def lib():
             "gbr_set_binning": [vp, u32],
             "gbr_set_predictor": [vp, vp, u32, C.c_float, C.c_float, C.c_float],
             "gbr_collect_bin_features": [vp, C.POINTER(Camera), u32, u32, u32, vp, vp, vp],
+            "gbr_predicted_capacities": [vp, vp, vp],
             "gbr_mlp_predict": [vp, vp, u32, vp, vp],
             "gbr_mlp_loss_grad": [vp, vp, vp, u32, vp, vp, vp],
             "gbr_mlp_adam": [vp, vp, vp, vp, vp, u32, C.c_float, C.c_float, vp],
@@ -336,6 +337,12 @@ class Renderer:
         """DrawTextureGlobal: the shader's sampler over the colour buffer."""
         check(self._lib.gbr_draw_texture_global(self.h, tex_id, 1 if stretch_to_window else 0, sample,
                                                 _stream(stream)))
+
+    def predicted_capacities(self, stream: int = 0) -> np.ndarray:
+        """Per-bin capacities of the last predicted-binning frame."""
+        out = np.empty(self.nbx * self.nby, np.uint32)
+        check(self._lib.gbr_predicted_capacities(self.h, _ptr(out), _stream(stream)))
+        return out
 
     def readback_ids(self, stream: int = 0) -> np.ndarray:
         ids = np.empty(self.width * self.height, np.uint32)

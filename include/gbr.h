@@ -180,6 +180,9 @@ void gbr_obj_free(gbr_obj_mesh *mesh);
  * parameters that also refreshes their BF16 copy. */
 gbr_status gbr_set_predictor(gbr_renderer *r, const uint16_t *weights_bf16, uint32_t num_params, float alpha,
                              float beta, float gamma);
+/* The per-bin capacities the model predicted for the last frame rendered
+ * with predicted binning (num_bins_x * num_bins_y values). */
+gbr_status gbr_predicted_capacities(gbr_renderer *r, uint32_t *capacities, void *stream);
 gbr_status gbr_collect_bin_features(gbr_renderer *r, const gbr_camera *cam, uint32_t cull, uint32_t sample,
                                     uint32_t vis, float *features, uint32_t *counts, void *stream);
 uint32_t gbr_mlp_num_params(void);

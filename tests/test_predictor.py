@@ -112,3 +112,42 @@ def test_predicted_binning_is_identical_to_exact(gbr_lib, cuda_device, count, ex
     for a, b in zip(exact[:5], pred[:5]):
         assert np.array_equal(a, b)
     assert pred[5]["num_pairs"] == exact[5]["num_pairs"] and pred[5]["num_visible"] == exact[5]["num_visible"]
+
+
+def bf16_round(a):
+    """float32 -> nearest-even BF16 -> float32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.gpu
+def test_tensor_core_capacities_match_the_model(gbr_lib, cuda_device):
+    """The capacity kernel runs the 12-64-64-1 model on the tensor cores
+    (tcgen05.mma, BF16 operands -- features and hidden layer rounded to
+    BF16 -- FP32 accumulation in tensor memory).  Its capacities match the
+    same model evaluated on the CPU with those roundings to within the
+    accumulation order (1% + 2 entries), on every bin."""
+    import predictor
+    s = scenes.soup_scene(150_000, 960, 540, 16, seed=9)
+    nb = s.num_bins_x * s.num_bins_y
+    feats = np.empty((nb, mlp_oracle.F), np.float32)
+    counts = np.empty(nb, np.uint32)
+    with gbr_lib.Renderer(s.width, s.height) as r:
+        r.load_scene(s)
+        cam = gbr_lib.make_camera(s.camera)
+        gbr_lib.check(r._lib.gbr_collect_bin_features(r.h, C.byref(cam), s.cull, s.sample, s.vis,
+                                                      feats.ctypes.data_as(C.c_void_p),
+                                                      counts.ctypes.data_as(C.c_void_p), None))
+        predictor.install(r)
+        r.render_scene(s)
+        r.stats()
+        caps = r.predicted_capacities().astype(np.float64)
+    w16, a, b, g, _ = predictor.load()
+    W1, b1, W2, b2, W3, b3 = (np.asarray(x, np.float32) for x in mlp_oracle.unpack(mlp_oracle.bf16_to_f64(w16)))
+    h1 = np.maximum(bf16_round(feats) @ W1 + b1, 0).astype(np.float32)
+    h2 = np.maximum(bf16_round(h1) @ W2 + b2, 0).astype(np.float32)
+    lam = mlp_oracle.softplus((h2 @ W3 + b3).astype(np.float64))
+    want = np.clip(np.ceil(lam * (1 + a) + b * np.sqrt(lam + 1) + g), 0, s.num_triangles)
+    assert caps.shape == want.shape
+    assert np.all(np.abs(caps - want) <= 0.01 * want + 2), float(np.max(np.abs(caps - want) - 0.01 * want))
