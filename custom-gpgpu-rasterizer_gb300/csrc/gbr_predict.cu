@@ -9,11 +9,14 @@
 //                    bin it accumulates the
 //                    sampled pair count, and per centroid bin the count,
 //                    bounding-box area (sum, max) and depth range;
-//   capacity_kernel  12 features per bin from those accumulators -> MLP
-//                    12-64-64-1 (ReLU, softplus out; parameters BF16, math
-//                    FP32) -> predicted count l -> capacity
+//   capacity_tc_kernel  12 features per bin from those accumulators -> MLP
+//                    12-64-64-1 (ReLU, softplus out) on the tensor cores:
+//                    tcgen05.mma with BF16 operands in shared memory and
+//                    FP32 accumulators in tensor memory, 128 bins per CTA
+//                    -> predicted count l -> capacity
 //                    ceil(l*(1+alpha) + beta*sqrt(l+1) + gamma), at most
-//                    the triangle count;
+//                    the triangle count (capacity_kernel, one warp per bin
+//                    with FP32 math, only collects the features);
 //   scan (capacities) -> one fused setup + fill pass appending inside each
 //                    bin's capacity -> a scan of the filled sizes builds the
 //                    raster work items (gbr_scan.cu, kScanPredictedItems).
