@@ -27,6 +27,7 @@ replicas, weak scaling); rank 0 prints the max-over-ranks line.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import re
@@ -94,12 +95,22 @@ def profile_traffic():
 
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms.
+
+    A timed region of a few milliseconds can fall between two samples, so
+    after the timed region `hold(step)` keeps running the same step (not
+    timed) until at least `min_samples` samples were taken since the timed
+    region began.  The report says how many samples fell inside the timed
+    region itself and how many frames the hold added."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
+        self.t0 = self.t1 = None
+        self.hold_frames = 0
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.FIELDS}",
@@ -107,33 +118,64 @@ class ClockSampler:
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        deadline = time.time() + 5.0
+        while self.p is not None and not self._rows() and time.time() < deadline:
+            time.sleep(0.05)
+
+    def _rows(self):
+        out = []
+        for line in open(self.f.name).read().strip().splitlines():
+            r = [x.strip() for x in line.split(",")]
+            if len(r) < len(self.FIELDS.split(",")):
+                continue
+            try:
+                ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                out.append((ts, float(r[2]), float(r[3]),
+                            [n for k, n in enumerate(self.REASONS) if r[6 + k].lower().startswith("active")]))
+            except ValueError:
+                continue
+        return out
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
+
+    def hold(self, step, min_samples: int = 3, limit_s: float = 5.0):
+        """Runs `step()` until `min_samples` samples are newer than begin()."""
+        if self.p is None or self.t0 is None:
+            return
+        deadline = time.time() + limit_s
+        while time.time() < deadline:
+            if sum(1 for r in self._rows() if r[0] >= self.t0 - 1e-3) >= min_samples:   # ms timestamps
+                break
+            step()
+            self.hold_frames += 1
 
     def stop(self):
         if self.p is None:
             return None
+        t_stop = time.time()
         self.p.terminate()
         try:
             self.p.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.p.kill()
         self.f.flush()
-        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        rows = self._rows()
         os.unlink(self.f.name)
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
-                for k, n in enumerate(names):
-                    if r[5 + k].strip().lower().startswith("active"):
-                        reasons.add(n)
-            except (ValueError, IndexError):
-                continue
-        if not sm:
+        t0 = self.t0 - 1e-3 if self.t0 is not None else 0.0   # timestamps are whole milliseconds
+        t1 = self.t1 if self.t1 is not None else t_stop
+        under_load = [r for r in rows if t0 <= r[0] <= t_stop]
+        if not under_load:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(r[1] for r in under_load),
+                "sm_max_mhz": max(r[2] for r in under_load),
+                "reasons": sorted({n for r in under_load for n in r[3]}),
+                "samples": len(under_load),
+                "samples_in_timed_region": sum(1 for r in under_load if r[0] <= t1),
+                "hold_frames": self.hold_frames}
 
 
 def cpu_baseline(scene, threads: int):
@@ -294,6 +336,7 @@ def run_ours(args, rank, world, local):
     sampler = ClockSampler(local)
     ms_total = []
     torch.cuda.synchronize(dev)
+    sampler.begin()
     with torch.cuda.stream(stream):
         for _ in range(args.steps):
             flush.zero_()
@@ -301,6 +344,14 @@ def run_ours(args, rank, world, local):
             st = r.stats(sptr)
             ms_total.append(st["ms_total"])
     torch.cuda.synchronize(dev)
+    sampler.end()
+
+    def frame():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            r.render_scene(scene, sptr)
+            r.stats(sptr)
+    sampler.hold(frame)
     clocks = sampler.stop()
     r.set_timing(True)
     predicted = predicted_binning(r, scene, args, stream, flush)
@@ -414,6 +465,7 @@ def run_icosphere(args, rank, world, local):
     sptr = stream.cuda_stream
     per_bins = {}
     sampler = ClockSampler(local)
+    sampler.begin()
     for bins in (8, 16):
         s = scenes.icosphere_lit_scene(bin_size=bins)
         with gbr.Renderer(s.width, s.height) as r:
@@ -431,6 +483,15 @@ def run_icosphere(args, rank, world, local):
                     r.render_scene(s, sptr)
                     st = r.stats(sptr)
                     ms.append(st["ms_total"])
+                torch.cuda.synchronize(dev)
+                if bins == 16:
+                    sampler.end()
+
+                    def frame():
+                        flush.zero_()
+                        r.render_scene(s, sptr)
+                        r.stats(sptr)
+                    sampler.hold(frame)
             per_bins[bins] = {"ms_frame": statistics.mean(ms), "pairs": int(st["num_pairs"]),
                               "visible": int(st["num_visible"]), "ms_setup": stages["ms_setup"],
                               "ms_bin": stages["ms_bin"], "ms_raster": stages["ms_raster"],
@@ -495,6 +556,7 @@ def run_batch(args, rank, world, local):
     torch.cuda.synchronize(dev)
     sampler = ClockSampler(local)
     ms = []
+    sampler.begin()
     with torch.cuda.stream(stream):
         for _ in range(args.steps):
             flush.zero_()
@@ -502,6 +564,14 @@ def run_batch(args, rank, world, local):
             st = b.stats(sptr)
             ms.append(st["ms_frame"])
     torch.cuda.synchronize(dev)
+    sampler.end()
+
+    def frame():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            b.render(sptr)
+            b.stats(sptr)
+    sampler.hold(frame)
     clocks = sampler.stop()
     t_batch = statistics.mean(ms) / 1e3
 
