@@ -133,6 +133,8 @@ uint64_t tri_count(uint32_t num_vertices, const uint32_t* indices, uint32_t num_
 
 void free_bins(gbr_renderer* r) {
     cudaFree(r->d_counts); cudaFree(r->d_sub_base); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
+    cudaFree(r->d_row_base);
+    r->d_row_base = nullptr;
     cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_scan);
     r->d_scan = nullptr;
     cudaFree(r->d_feat); cudaFree(r->d_features_out);
@@ -285,6 +287,14 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.cap_alpha = r->cap_alpha; F.cap_beta = r->cap_beta; F.cap_gamma = r->cap_gamma;
     F.sample_stride = kSampleStride;
     F.exact_guard = predicted ? 1u : 0u;
+    // exact binning of a dense frame: block-private counter rows
+    const uint32_t rows = std::min<uint32_t>((F.num_tris + kRowThreads - 1u) / kRowThreads, (uint32_t)r->num_sms);
+    if (!predicted && r->d_row_base && use_count_rows(r->seen_pairs, nb, rows)) {
+        F.row_base = r->d_row_base;
+        F.row_blocks = rows;
+        F.count_split = 1u;
+    }
+    r->last_row_blocks = F.row_blocks;
 
     const bool stages = r->timing == GBR_TIMING_STAGES;
     if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[0], s));
@@ -435,6 +445,8 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     GBR_CUDA(cudaMalloc(&r->d_counts, (size_t)kCountSplit * nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_counts, 0, (size_t)kCountSplit * nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_sub_base, (size_t)kCountSplit * nb * sizeof(uint32_t)));
+    if (nb <= kMaxRowBins && r->num_sms > 0)
+        GBR_CUDA(cudaMalloc(&r->d_row_base, (size_t)r->num_sms * nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_offsets, (nb + 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_offsets, 0, (nb + 1u) * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_cursors, nb * sizeof(uint32_t)));
@@ -789,6 +801,7 @@ gbr_status gbr_get_stats(gbr_renderer* r, gbr_stats* out, void* stream) {
     out->num_float_path = r->h_ctl->num_float_path;
     out->predicted_overflow = r->h_ctl->pred_overflow;
     out->predicted_capacity = r->h_ctl->pred_capacity;
+    out->count_blocks = r->last_row_blocks;
     out->ms_setup = out->ms_bin = out->ms_raster = out->ms_shade = out->ms_total = 0.f;
     if (r->timing == GBR_TIMING_TOTAL && r->ev_recorded) {
         cudaEventElapsedTime(&out->ms_total, r->ev[0], r->ev[3]);

@@ -38,6 +38,18 @@ __host__ __device__ inline uint32_t count_split_for(unsigned long long pairs, ui
     return per_bin >= 256u ? 8u : per_bin >= 64u ? 4u : per_bin >= 16u ? 2u : 1u;
 }
 constexpr uint32_t kDefaultRasterCtas = 6;        // raster_kernel variant (CTAs per SM) used by default
+// Exact binning with block-private counter rows: one block of kRowThreads
+// per SM counts its pairs per bin in shared memory (num_bins <=
+// kMaxRowBins), then takes its run of every bin it touched with one global
+// atomic per bin; the fill pass, the same blocks over the same triangles,
+// hands out the runs' slots from shared memory.  Used once a frame has shown
+// at least one pair per (block, bin) on average; sparser frames keep the
+// global sub-counters.
+constexpr uint32_t kRowThreads = 1024;
+constexpr uint32_t kMaxRowBins = 32768;
+__host__ __device__ inline bool use_count_rows(unsigned long long pairs, uint32_t bins, uint32_t blocks) {
+    return bins > 0u && bins <= kMaxRowBins && blocks > 0u && pairs >= (unsigned long long)bins * blocks;
+}
 
 enum : uint32_t { kVertexIVertex56 = 0, kVertexPos3Rgba8 = 1 };
 
@@ -153,6 +165,10 @@ struct FrameDev {
     unsigned long long rank_cap;
     uint32_t count_stride;     // bins between sub-counter rows (the scan's bin count)
     uint32_t count_split;      // sub-counters per bin in use: 1, 2, 4 or 8
+    // exact binning with block-private counter rows (row_blocks > 0)
+    uint32_t* row_base;        // row_blocks x num_bins: a block's first entry in each bin it touched, bin-relative
+    uint32_t row_blocks;       // blocks of the count and fill passes (0: sub-counters)
+    uint32_t row_pad;
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -437,7 +453,7 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
 }
 
 // Walks the bins of the warp's packed rectangles; called by whole warps of
-// 256-thread blocks.  The warp's (triangle, bin) pairs are expanded
+// 256-thread blocks (kRowThreads blocks in modes 4 and 5).  The warp's (triangle, bin) pairs are expanded
 // load-balanced, 32 consecutive pairs per round: the lane whose pair range
 // covers the round's first pair is found with a ballot, the starts of the
 // other ranges inside the round with one OR-reduction, and a lane's pair
@@ -449,7 +465,9 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
 // Mode 0: count (atomicAdd on the walk's sub-counter of the bin; its return,
 // the pair's rank there, is kept in the walk's rank slots), 1: fill (entry
 // at the sub-counter's list start + rank: no atomics), 2: predicted fill (append within the bin's predicted
-// capacity), 3: pre-pass count (atomicAdd on the first feature slot).  A
+// capacity), 3: pre-pass count (atomicAdd on the first feature slot),
+// 4: count into the block's shared-memory row `s_row` (no return), 5: fill
+// from the block's shared-memory cursors `s_row` (kRowThreads blocks).  A
 // walk is identified by `walk` (its first triangle slot / 32), so the count
 // and fill passes of the same triangles meet the same slots.  One atomic per
 // pair: merging the atomics of same-bin lanes -- every such lane of the warp
@@ -461,8 +479,10 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
 constexpr uint32_t kPairsPerLane = GBR_PAIRS_PER_LANE;
 
 template <int MODE>
-__device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid, uint32_t walk) {
-    __shared__ uint4 s_tab[8][32];   // per warp: (first pair, width, bx0 | by0 << 16, entry) of each lane
+__device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t entry, bool valid, uint32_t walk,
+                                         uint32_t* s_row = nullptr) {
+    constexpr uint32_t kWarps = MODE >= 4 ? kRowThreads / 32u : 8u;
+    __shared__ uint4 s_tab[kWarps][32];   // per warp: (first pair, width, bx0 | by0 << 16, entry) of each lane
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t bx0 = rect.x & 0xFFFFu, bx1 = rect.x >> 16;
     const uint32_t by0 = rect.y & 0xFFFFu, by1 = (rect.y >> 16) & 0x7FFFu;
@@ -525,6 +545,17 @@ __device__ __forceinline__ void bin_walk(const FrameDev& F, uint2 rect, uint32_t
 #pragma unroll
             for (uint32_t u = 0; u < kPairsPerLane; ++u)
                 if (act[u]) atomicAdd(&F.feat[bin[u]], 1u);
+        } else if (MODE == 4) {
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u)
+                if (act[u]) atomicAdd(&s_row[bin[u]], 1u);
+        } else if (MODE == 5) {
+            uint32_t pos[kPairsPerLane];
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u) pos[u] = act[u] ? atomicAdd(&s_row[bin[u]], 1u) : 0u;
+#pragma unroll
+            for (uint32_t u = 0; u < kPairsPerLane; ++u)
+                if (act[u]) F.list[pos[u]] = ent[u];
         } else if (MODE == 0) {
             // count, keeping the pair's rank within its bin (slots past the
             // storage are dropped: that frame overflows and is not filled)

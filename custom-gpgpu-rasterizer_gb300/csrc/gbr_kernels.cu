@@ -67,11 +67,13 @@ __device__ __forceinline__ uint32_t hiz_key(const TriSetup& t) {
 
 // Vertex stage (positions), triangle assembly, cull, frustum reject, raster
 // setup record, depth-key bound and bin rectangle of triangle `prim`, then the count pass
-// (MODE 0) or the predicted-capacity fill (MODE 1).  Called by whole warps.
+// (MODE 0), the predicted-capacity fill (MODE 1) or the count into the
+// block's shared-memory row `s_row` (MODE 2).  Called by whole warps.
 // Returns the warp's visible and float-path triangle counts (bits 0-15 and
 // 16-31), for the block's statistics.
 template <int MODE>
-__device__ __forceinline__ uint32_t setup_tri(const FrameDev& F, uint32_t prim, uint32_t walk) {
+__device__ __forceinline__ uint32_t setup_tri(const FrameDev& F, uint32_t prim, uint32_t walk,
+                                              uint32_t* s_row = nullptr) {
     const bool in_range = prim < F.num_tris;
     uint2 rect = empty_rect();
     bool visible = false, fpath = false, no_raster = true;
@@ -147,6 +149,7 @@ __device__ __forceinline__ uint32_t setup_tri(const FrameDev& F, uint32_t prim, 
     const uint32_t counts = (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, visible)) |
                             ((uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, fpath)) << 16);
     if (MODE == 0) bin_walk<0>(F, rect, 0u, visible, walk);
+    else if (MODE == 2) bin_walk<4>(F, rect, 0u, visible, walk, s_row);
     else bin_walk<2>(F, rect, prim | (no_raster ? kNoRasterBit : 0u), visible, walk);
     return counts;
 }
@@ -200,6 +203,60 @@ __global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
     if (F.ctl->overflow || (F.exact_guard && !F.ctl->pred_overflow)) return;
     for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x)
         fill_tri(F, base + threadIdx.x, (base + threadIdx.x) >> 5);
+    pdl_release();
+}
+
+// Exact binning with block-private counter rows (num_bins <= kMaxRowBins,
+// one kRowThreads block per SM, F.row_blocks blocks).  The count pass counts
+// the block's pairs per bin in shared memory, then takes the block's run of
+// each bin it touched with one global atomic per bin (blocks start their
+// sweep at different bins, so the blocks' atomics on one bin do not arrive
+// together); the run's start, relative to the bin, goes to the block's row
+// of F.row_base.
+__global__ void __launch_bounds__(kRowThreads, 1) setup_rows_kernel(FrameDev F) {
+    extern __shared__ uint32_t s_row[];
+    pdl_wait();
+    const uint32_t nb = F.num_bins;
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) s_row[b] = 0u;
+    __syncthreads();
+    uint32_t vis = 0, fp = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x) {
+        const uint32_t c = setup_tri<2>(F, base + threadIdx.x, (base + threadIdx.x) >> 5, s_row);
+        vis += c & 0xFFFFu;
+        fp += c >> 16;
+    }
+    __syncthreads();
+    uint32_t* const row = F.row_base + (size_t)blockIdx.x * nb;
+    const uint32_t shift = (uint32_t)(((unsigned long long)blockIdx.x * nb) / gridDim.x);
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) {
+        uint32_t b = i + shift;
+        if (b >= nb) b -= nb;
+        const uint32_t c = s_row[b];
+        if (c) row[b] = atomicAdd(&F.counts[b], c);
+    }
+    add_block_stats(F.ctl, vis, fp);
+    pdl_release();
+}
+
+// The fill pass of block-private rows: the same blocks walk the same
+// triangles; each bin's cursor starts at the bin's offset plus the block's
+// run start, and every pair takes the next slot with a shared-memory atomic.
+// Cursors of bins the block never touched hold unused values.
+__global__ void __launch_bounds__(kRowThreads, 1) fill_rows_kernel(FrameDev F) {
+    extern __shared__ uint32_t s_row[];
+    pdl_wait();
+    if (F.ctl->overflow) return;
+    const uint32_t nb = F.num_bins;
+    const uint32_t* const row = F.row_base + (size_t)blockIdx.x * nb;
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) s_row[b] = __ldg(F.offsets + b) + __ldg(row + b);
+    __syncthreads();
+    for (uint32_t base = blockIdx.x * blockDim.x; base < F.num_tris; base += gridDim.x * blockDim.x) {
+        const uint32_t prim = base + threadIdx.x;
+        const bool in_range = prim < F.num_tris;
+        const uint2 rect = in_range ? F.rects[prim] : empty_rect();
+        const uint32_t entry = prim | ((rect.y & 0x80000000u) ? kNoRasterBit : 0u);
+        bin_walk<5>(F, rect, entry, in_range, prim >> 5, s_row);
+    }
     pdl_release();
 }
 
@@ -620,7 +677,7 @@ size_t raster_smem_bytes(uint32_t bw, uint32_t bh) {
 // does not run costs one grid of early exits; more blocks than are resident
 // at once (the setup pass holds 5 per SM) balance uneven triangles better
 // than exactly one wave (measured ~9% faster for the 1M soup).
-static uint32_t triangle_blocks(uint32_t num_tris) {
+static int sm_count() {
     static int sms = 0;
     if (sms <= 0) {
         int dev = 0;
@@ -629,10 +686,35 @@ static uint32_t triangle_blocks(uint32_t num_tris) {
             sms = 152;
         }
     }
-    return std::min<uint32_t>((num_tris + 255u) / 256u, 8u * (uint32_t)sms);
+    return sms;
+}
+
+static uint32_t triangle_blocks(uint32_t num_tris) {
+    return std::min<uint32_t>((num_tris + 255u) / 256u, 8u * (uint32_t)sm_count());
+}
+
+// Dynamic shared memory of the block-row kernels: one counter per bin (the
+// opt-in above the default 48 KB is made once per process).
+static cudaError_t row_smem(const FrameDev& F, size_t* bytes) {
+    static bool opted = false;
+    *bytes = (size_t)F.num_bins * sizeof(uint32_t);
+    if (!opted) {
+        const int most = (int)(kMaxRowBins * sizeof(uint32_t));
+        cudaError_t e = cudaFuncSetAttribute(setup_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(fill_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        if (e != cudaSuccess) return e;
+        opted = true;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s) {
+    if (!predicted && F.row_blocks) {
+        size_t smem = 0;
+        const cudaError_t e = row_smem(F, &smem);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(setup_rows_kernel, dim3(F.row_blocks), dim3(kRowThreads), smem, s, F);
+    }
     const uint32_t blocks = triangle_blocks(F.num_tris);
     if (blocks == 0) return cudaSuccess;
     return predicted ? launch_pdl(setup_kernel<1>, dim3(blocks), dim3(256), 0, s, F)
@@ -640,6 +722,12 @@ cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s) {
 }
 
 cudaError_t launch_fill(const FrameDev& F, cudaStream_t s) {
+    if (F.row_blocks) {
+        size_t smem = 0;
+        const cudaError_t e = row_smem(F, &smem);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(fill_rows_kernel, dim3(F.row_blocks), dim3(kRowThreads), smem, s, F);
+    }
     const uint32_t blocks = triangle_blocks(F.num_tris);
     if (blocks == 0) return cudaSuccess;
     return launch_pdl(fill_kernel, dim3(blocks), dim3(256), 0, s, F);

@@ -77,7 +77,8 @@ typedef struct {
     uint64_t predicted_capacity; /* sum of predicted per-bin capacities, last frame */
     float ms_setup, ms_bin, ms_raster, ms_total; /* per-stage times of the last frame with timing on */
     float ms_shade;              /* the shade pass (included in ms_total, not in ms_raster) */
-    float pad;
+    uint32_t count_blocks;       /* blocks with private counter rows in the last frame's exact
+                                    count pass (0: per-bin counters in global memory) */
 } gbr_stats;
 
 /* CUDARenderer(const WindowHelper&) (CUDARenderer.cu:33-46): headless, the

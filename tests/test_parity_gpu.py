@@ -270,4 +270,43 @@ def test_full_size_soup_1m_1080p(gbr_lib, cuda_device):
     mask = (binidx % stride) == 7
     assert_matches_fixed(g, osub, mask)
     assert g["stats"]["num_pairs"] == ob["stats"]["num_pairs"]
-    g["renderer"].close()
+    # the second frame counts in block-private rows (the first frame showed
+    # about 6 pairs per (block, bin)): same lists, same image
+    r = g["renderer"]
+    assert g["stats"]["count_blocks"] == 0
+    r.render_scene(s)
+    offsets, bins = r.get_bins()
+    colour, depth = r.readback()
+    st = r.stats()
+    assert st["count_blocks"] > 0
+    assert_bins_equal({"offsets": offsets, "bins": bins}, ob)
+    assert np.array_equal(colour, g["colour"]) and np.array_equal(r.readback_ids(), g["ids"])
+    r.close()
+
+
+@pytest.mark.parametrize("bins,n,cull", [(8, 50_000, scenes.CULL_NONE), (32, 120_000, scenes.CULL_BACKFACE),
+                                         (24, 30_000, scenes.CULL_NONE)])
+def test_block_counter_rows(gbr_lib, cuda_device, bins, n, cull):
+    """Exact binning with block-private counter rows, taken once a frame has
+    shown at least one (triangle, bin) pair per (block, bin): the second
+    frame's bin lists, winners, depth and colour against the oracle."""
+    s = scenes.soup_scene(n, 640, 480, bin_size=bins, seed=5, cull=cull)
+    r = gbr_lib.Renderer(s.width, s.height)
+    first = gpu_render(gbr_lib, s, 64, renderer=r)
+    assert first["stats"]["count_blocks"] == 0
+    r.render_scene(s)
+    offsets, bl = r.get_bins()
+    colour, depth = r.readback()
+    g = {"offsets": offsets, "bins": bl, "colour": colour, "depth": depth, "ids": r.readback_ids()}
+    st = r.stats()
+    assert st["count_blocks"] == min((n + 1023) // 1024, cuda_device_sms())
+    o = oracle.render(s, oracle.RASTER_FIXED)
+    assert_bins_equal(g, o)
+    assert_matches_fixed(g, o)
+    assert st["num_pairs"] == o["stats"]["num_pairs"] and st["num_visible"] == o["stats"]["num_visible"]
+    r.close()
+
+
+def cuda_device_sms():
+    import torch
+    return torch.cuda.get_device_properties(0).multi_processor_count
