@@ -297,6 +297,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     r->last_row_blocks = F.row_blocks;
 
     const bool stages = r->timing == GBR_TIMING_STAGES;
+    const bool touch = r->seen_pairs >= kListTouchMinPairs;
     if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[0], s));
     GBR_CUDA(cudaMemsetAsync(r->d_ctl, 0, sizeof(Ctl), s));
     if (predicted) {
@@ -320,6 +321,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         GBR_CUDA(launch_setup(F, false, s));
         if (stages) GBR_CUDA(cudaEventRecord(r->ev[1], s));
         GBR_CUDA(launch_scan(scan_of(F, kScanExact), s));
+        if (touch) GBR_CUDA(launch_list_touch(F, false, s));
         GBR_CUDA(launch_fill(F, s));
     }
     r->last_predicted = predicted;
