@@ -321,7 +321,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         GBR_CUDA(launch_setup(F, false, s));
         if (stages) GBR_CUDA(cudaEventRecord(r->ev[1], s));
         GBR_CUDA(launch_scan(scan_of(F, kScanExact), s));
-        if (touch) GBR_CUDA(launch_list_touch(F, false, s));
+        if (touch) GBR_CUDA(launch_list_touch(F, s));
         GBR_CUDA(launch_fill(F, s));
     }
     r->last_predicted = predicted;

@@ -5,10 +5,17 @@
 //                  rectangle, and the count pass of exact binning (one
 //                  atomic per (triangle, bin) pair, whose return -- the pair's
 //                  rank in its bin -- is kept).
+//   setup_rows_kernel: the same with block-private counter rows (dense
+//                  frames): pairs counted per bin in shared memory, one
+//                  global atomic per (block, bin) reserves the block's run.
 //   scan_kernel  : (gbr_scan.cu) bin counts -> list offsets and raster work
 //                  items (bin, chunk of <= queue_chunk ids).
+//   list_touch_kernel: zeros the frame's list entries in whole words so the
+//                  fill's scattered stores merge in L2 (frames of >= 2^20
+//                  pairs).
 //   fill_kernel  : second pass: each pair's id goes to its bin's offset +
-//                  rank, no atomics.
+//                  rank, no atomics (fill_rows_kernel: to the block's run,
+//                  slots from shared-memory cursors).
 //   raster_kernel: persistent CTAs pull work items; a CTA depth-sorts its
 //                  chunk by the key bounds, rasterises front to back into a
 //                  shared-memory tile of packed (depth key, prim id) with
@@ -272,24 +279,16 @@ __global__ void __launch_bounds__(kRowThreads, 1) fill_rows_kernel(FrameDev F) {
     pdl_release();
 }
 
-// Zeros over the frame's bin-list entries in whole 16-byte words, before a
-// fill pass scatters its 4-byte stores there: [0, num_pairs) for exact
-// binning, [0, predicted capacity) before the predicted fused pass.  The
+// Zeros over the frame's bin-list entries [0, num_pairs) in whole 16-byte
+// words, before the exact fill pass scatters its 4-byte stores there.  The
 // list's sectors are then fully written in L2, and the scattered stores
 // merge into them instead of each partly written sector being completed
-// from DRAM (1M soup: exact scan + fill 84 -> 64 us with this pass).  The
-// predicted fused pass, bound by its returning atomics, gains nothing and
-// the library does not touch its list.
-__global__ void __launch_bounds__(256) list_touch_kernel(FrameDev F, bool predicted) {
+// from DRAM (1M soup: scan + fill 84 -> 64 us with this pass).  The
+// predicted fused pass, bound by its returning atomics, measured no gain.
+__global__ void __launch_bounds__(256) list_touch_kernel(FrameDev F) {
     pdl_wait();
-    unsigned long long n = 0;
-    if (predicted) {
-        if (!F.ctl->pred_overflow) n = F.ctl->pred_capacity;
-    } else if (!F.ctl->overflow) {
-        n = F.ctl->num_pairs;
-    }
-    n = min(n, F.list_cap);
-    {
+    if (!F.ctl->overflow) {
+        const unsigned long long n = min((unsigned long long)F.ctl->num_pairs, F.list_cap);
         uint4* const p = reinterpret_cast<uint4*>(F.list);
         const unsigned long long words = (n + 3u) / 4u;   // list storage is 2 x list_cap entries
         for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < words;
@@ -299,8 +298,8 @@ __global__ void __launch_bounds__(256) list_touch_kernel(FrameDev F, bool predic
     pdl_release();
 }
 
-cudaError_t launch_list_touch(const FrameDev& F, bool predicted, cudaStream_t s) {
-    return launch_pdl(list_touch_kernel, dim3(4u * (uint32_t)sm_count()), dim3(256), 0, s, F, predicted);
+cudaError_t launch_list_touch(const FrameDev& F, cudaStream_t s) {
+    return launch_pdl(list_touch_kernel, dim3(4u * (uint32_t)sm_count()), dim3(256), 0, s, F);
 }
 
 // ---------------------------------------------------------------------------

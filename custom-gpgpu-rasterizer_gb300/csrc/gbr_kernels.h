@@ -43,7 +43,7 @@ cudaError_t launch_fill(const FrameDev& F, cudaStream_t s);
 // Zeros the frame's list entries ahead of a scattering fill pass (see
 // list_touch_kernel); worth its launch once a frame holds ~1M entries.
 constexpr unsigned long long kListTouchMinPairs = 1ull << 20;
-cudaError_t launch_list_touch(const FrameDev& F, bool predicted, cudaStream_t s);
+cudaError_t launch_list_touch(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s);
 cudaError_t launch_shade(const FrameDev& F, cudaStream_t s);
 cudaError_t launch_clear(const FrameDev& F, cudaStream_t s);
