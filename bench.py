@@ -510,7 +510,8 @@ def run_icosphere(args, rank, world, local):
                                      "resolution": [3840, 2160], "best_bins": best,
                                      "bins_8x8": per_bins[8], "bins_16x16": per_bins[16],
                                      "l2": "256 MB write between timed frames"},
-                          "gpu_launches": 5 * args.steps * 2, "clocks": clocks}), flush=True)
+                          # setup, scan, fill, raster, shade queue, shade; two bin sizes
+                          "gpu_launches": 6 * args.steps * 2, "clocks": clocks}), flush=True)
 
 
 BATCH_SCENES = 256

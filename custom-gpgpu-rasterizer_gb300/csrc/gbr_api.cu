@@ -295,6 +295,12 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         F.count_split = 1u;
     }
     r->last_row_blocks = F.row_blocks;
+    // frames shaded through the full vertex stage shade their covered
+    // pixels in a second, densely packed pass
+    if (!F.flat_shade && vis != GBR_VIS_DEPTH) {
+        if (!r->d_shade_list) GBR_CUDA(cudaMalloc(&r->d_shade_list, (size_t)r->W * r->H * sizeof(uint32_t)));
+        F.shade_list = r->d_shade_list;
+    }
 
     const bool stages = r->timing == GBR_TIMING_STAGES;
     const bool touch = r->seen_pairs >= kListTouchMinPairs;
@@ -420,7 +426,7 @@ gbr_status gbr_destroy(gbr_renderer* r) {
     gbr_scene_clear(r);
     for (TexHost& t : r->textures) free_texture(t);
     free_bins(r);
-    cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis);
+    cudaFree(r->d_colour); cudaFree(r->d_depth); cudaFree(r->d_ids); cudaFree(r->d_gvis); cudaFree(r->d_shade_list);
     cudaFree(r->d_setup); cudaFree(r->d_rects); cudaFree(r->d_walk); cudaFree(r->d_keys); cudaFree(r->d_meshes); cudaFree(r->d_ctl); cudaFree(r->d_mlp_w);
     cudaFree(r->d_lights);
     cudaFreeHost(r->h_meshes); cudaFreeHost(r->h_ctl);

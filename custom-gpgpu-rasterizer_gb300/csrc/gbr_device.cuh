@@ -112,7 +112,7 @@ struct Ctl {
     uint32_t num_sampled;      // visible triangles seen by the coarse pre-pass
     unsigned long long items_alloc;   // batch: work items requested by all scenes
     uint32_t rank_next;        // exact binning: rank slots reserved by the count pass
-    uint32_t pad;
+    uint32_t shade_count;      // two-pass shading: covered pixels queued by the light pass
 };
 static_assert(sizeof(Ctl) == 64, "control block is 64 bytes");
 
@@ -169,6 +169,8 @@ struct FrameDev {
     uint32_t* row_base;        // row_blocks x num_bins: a block's first entry in each bin it touched, bin-relative
     uint32_t row_blocks;       // blocks of the count and fill passes (0: sub-counters)
     uint32_t row_pad;
+    uint32_t* shade_list;      // two-pass shading: covered pixels' indices, width x height slots (null: one pass)
+    uint32_t shade_pad[2];
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 

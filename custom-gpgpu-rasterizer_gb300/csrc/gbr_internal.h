@@ -81,6 +81,7 @@ struct gbr_renderer {
     float* d_depth = nullptr;
     uint32_t* d_ids = nullptr;
     unsigned long long* d_gvis = nullptr;
+    uint32_t* d_shade_list = nullptr;   // two-pass shading queue, W x H (allocated on first use)
 
     uint32_t* d_counts = nullptr;     // kCountSplit x bins
     uint32_t* d_sub_base = nullptr;   // kCountSplit x bins

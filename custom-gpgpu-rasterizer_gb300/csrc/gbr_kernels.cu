@@ -400,13 +400,17 @@ __device__ __noinline__ void raster_float(const TriSetup& t, uint32_t prim, unsi
     }
 }
 
+__device__ __forceinline__ void clear_pixel(const FrameDev& F, size_t gi) {
+    F.colour[gi] = F.vis == 0u ? F.clear_colour32 : 0u;
+    F.depth[gi] = 0.f;
+    F.ids[gi] = kInvalidPrim;
+}
+
 template <bool FLAT>
 __device__ __forceinline__ void resolve_pixel(const FrameDev& F, int x, int y, unsigned long long v) {
     const size_t gi = (size_t)y * F.width + (size_t)x;
     if (v == kEmptyVis) {
-        F.colour[gi] = F.vis == 0u ? F.clear_colour32 : 0u;
-        F.depth[gi] = 0.f;
-        F.ids[gi] = kInvalidPrim;
+        clear_pixel(F, gi);
         return;
     }
     const uint32_t prim = (uint32_t)(v & 0xFFFFFFFFull);
@@ -633,6 +637,45 @@ __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
     shade_px<FLAT>(F, i);
 }
 
+// Two-pass shading, for frames that shade through the full vertex stage
+// (textured or lit meshes, the normal view).  The light pass clears the
+// pixels no triangle won and queues the covered ones; the heavy pass shades
+// the queue, 32 covered pixels to a warp, over the whole GPU.  In one pass
+// a covered region's pixels sit a few to a warp inside blocks that keep
+// their SM slot for the whole shading chain (4K icosphere: 140K covered
+// pixels of 8.3M).
+__global__ void __launch_bounds__(256) shade_queue_kernel(FrameDev F) {
+    pdl_wait();
+    if (F.ctl->overflow) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool covered = false;
+    if (i < F.width * F.height) {
+        covered = F.gvis[i] != kEmptyVis;
+        if (!covered) clear_pixel(F, i);
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, covered);
+    if (m) {
+        const uint32_t lane = threadIdx.x & 31u, leader = (uint32_t)__ffs(m) - 1u;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&F.ctl->shade_count, (uint32_t)__popc(m));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (covered) F.shade_list[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = i;
+    }
+    pdl_release();
+}
+
+__global__ void __launch_bounds__(256) shade_list_kernel(FrameDev F) {
+    pdl_wait();
+    if (F.ctl->overflow) return;
+    const uint32_t count = F.ctl->shade_count;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+        const uint32_t i = __ldg(F.shade_list + j);
+        const unsigned long long v = F.gvis[i];
+        F.gvis[i] = kEmptyVis;
+        resolve_pixel<false>(F, (int)(i % F.width), (int)(i / F.width), v);
+    }
+}
+
 // Pixels no bin covers (num_bins * bin_dim smaller than the screen).
 __global__ void clear_kernel(FrameDev F) {
     const size_t n = (size_t)F.width * F.height;
@@ -786,6 +829,18 @@ cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
 cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
     const uint32_t npx = F.width * F.height;
     const dim3 g((npx + 255u) / 256u), b(256);
+    if (!F.flat_shade && F.shade_list) {
+        const cudaError_t e = launch_pdl(shade_queue_kernel, g, b, 0, s, F);
+        if (e != cudaSuccess) return e;
+        // one resident wave: the queue is a few pixels per thread at most
+        static int per_sm = 0;
+        if (per_sm <= 0 &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shade_list_kernel, 256, 0) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = 2;
+        }
+        return launch_pdl(shade_list_kernel, dim3((uint32_t)std::max(per_sm, 1) * (uint32_t)sm_count()), b, 0, s, F);
+    }
     return F.flat_shade ? launch_pdl(shade_kernel<true>, g, b, 0, s, F) : launch_pdl(shade_kernel<false>, g, b, 0, s, F);
 }
 
