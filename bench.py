@@ -641,13 +641,28 @@ def run_batch(args, rank, world, local):
     return line
 
 
-def profile_frames(n: int, binning: str = "exact"):
+def profile_frames(n: int, binning: str = "exact", workload: str = "soup"):
     """The benchmark's frame, device resident, n times on the default stream
-    (with the committed capacity model when binning is "predicted")."""
+    (with the committed capacity model when binning is "predicted"); with
+    workload "icosphere" the lit 4K icosphere frame with 16x16 bins."""
     import torch
     import gbr
 
     dev = torch.device("cuda", 0)
+    if workload == "icosphere":
+        import scenes
+        s = scenes.icosphere_lit_scene(bin_size=16)
+        r = gbr.Renderer(s.width, s.height)
+        r.load_scene(s, CHUNK)
+        for i in range(n):
+            r.render_scene(s)
+            if i == 0:
+                r.stats()
+        st = r.stats()
+        torch.cuda.synchronize(dev)
+        r.close()
+        print(json.dumps({"frames": n, "pairs": st["num_pairs"], "visible": st["num_visible"]}))
+        return
     scene = make_scene(0)
     mesh = scene.meshes[0]
     d_vert = torch.from_numpy(mesh.vertices.view(np.uint8)).to(dev)
@@ -686,7 +701,7 @@ def main():
     if args.profile_frames:
         import build as gbr_build
         gbr_build.build()
-        profile_frames(args.profile_frames, args.binning)
+        profile_frames(args.profile_frames, args.binning, args.workload)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -644,27 +644,64 @@ __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
 // a covered region's pixels sit a few to a warp inside blocks that keep
 // their SM slot for the whole shading chain (4K icosphere: 140K covered
 // pixels of 8.3M).
+//
+// Light pass: one thread per 4 consecutive pixels: their merge words come in with two
+// 16-byte loads, an all-empty quad (most of a frame whose geometry covers a
+// small part of the screen) is cleared with 16-byte stores, and a warp
+// queues its covered pixels with one atomic.  Buffers not 16-byte aligned
+// take per-pixel accesses.
 __global__ void __launch_bounds__(256) shade_queue_kernel(FrameDev F) {
     pdl_wait();
     if (F.ctl->overflow) return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool covered = false;
-    if (i < F.width * F.height) {
-        covered = F.gvis[i] != kEmptyVis;
-        if (!covered) clear_pixel(F, i);
+    const uint32_t n = F.width * F.height, lane = threadIdx.x & 31u;
+    const uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(F.gvis) | reinterpret_cast<uintptr_t>(F.colour) |
+                           reinterpret_cast<uintptr_t>(F.depth) | reinterpret_cast<uintptr_t>(F.ids)) & 15u) == 0u;
+    uint32_t covered = 0;   // bit k: pixel i0 + k has a winner
+    if (aligned && i0 + 4u <= n) {
+        const ulonglong2* g = reinterpret_cast<const ulonglong2*>(F.gvis + i0);
+        const ulonglong2 a = g[0], b = g[1];
+        covered = (a.x != kEmptyVis ? 1u : 0u) | (a.y != kEmptyVis ? 2u : 0u) | (b.x != kEmptyVis ? 4u : 0u) |
+                  (b.y != kEmptyVis ? 8u : 0u);
+        if (covered == 0u) {
+            const uint32_t c = F.vis == 0u ? F.clear_colour32 : 0u;
+            *reinterpret_cast<uint4*>(F.colour + i0) = make_uint4(c, c, c, c);
+            *reinterpret_cast<float4*>(F.depth + i0) = make_float4(0.f, 0.f, 0.f, 0.f);
+            *reinterpret_cast<uint4*>(F.ids + i0) = make_uint4(kInvalidPrim, kInvalidPrim, kInvalidPrim, kInvalidPrim);
+        } else {
+            for (uint32_t k = 0; k < 4u; ++k)
+                if (!((covered >> k) & 1u)) clear_pixel(F, i0 + k);
+        }
+    } else {
+        for (uint32_t k = 0; k < 4u && i0 + k < n; ++k) {
+            if (F.gvis[i0 + k] != kEmptyVis) covered |= 1u << k;
+            else clear_pixel(F, i0 + k);
+        }
     }
-    const uint32_t m = __ballot_sync(0xFFFFFFFFu, covered);
-    if (m) {
-        const uint32_t lane = threadIdx.x & 31u, leader = (uint32_t)__ffs(m) - 1u;
+    // the warp's covered pixels go to the queue in one run
+    const uint32_t c = (uint32_t)__popc(covered);
+    uint32_t incl = c;
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (total) {
         uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&F.ctl->shade_count, (uint32_t)__popc(m));
-        base = __shfl_sync(0xFFFFFFFFu, base, leader);
-        if (covered) F.shade_list[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = i;
+        if (lane == 31u) base = atomicAdd(&F.ctl->shade_count, total);
+        base = __shfl_sync(0xFFFFFFFFu, base, 31);
+        uint32_t at = base + incl - c;
+        for (uint32_t k = 0; k < 4u; ++k)
+            if ((covered >> k) & 1u) F.shade_list[at++] = i0 + k;
     }
     pdl_release();
 }
 
-__global__ void __launch_bounds__(256) shade_list_kernel(FrameDev F) {
+// 4 blocks per SM (<= 64 registers): the heavy pass is bound by the latency
+// of its dependent loads, and a 4K frame's covered pixels then fit in one
+// resident wave (3 blocks per SM at 80 registers: 71.7 -> 63.5 us with 4).
+__global__ void __launch_bounds__(256, 4) shade_list_kernel(FrameDev F) {
     pdl_wait();
     if (F.ctl->overflow) return;
     const uint32_t count = F.ctl->shade_count;
@@ -830,7 +867,7 @@ cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
     const uint32_t npx = F.width * F.height;
     const dim3 g((npx + 255u) / 256u), b(256);
     if (!F.flat_shade && F.shade_list) {
-        const cudaError_t e = launch_pdl(shade_queue_kernel, g, b, 0, s, F);
+        const cudaError_t e = launch_pdl(shade_queue_kernel, dim3((npx + 1023u) / 1024u), b, 0, s, F);
         if (e != cudaSuccess) return e;
         // one resident wave: the queue is a few pixels per thread at most
         static int per_sm = 0;
