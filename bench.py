@@ -649,6 +649,26 @@ def profile_frames(n: int, binning: str = "exact", workload: str = "soup"):
     import gbr
 
     dev = torch.device("cuda", 0)
+    if workload == "batch":
+        import scenes
+        sl = scenes.batch_scenes(BATCH_SCENES, seed=0)
+        rs = []
+        b = gbr.Batch()
+        for s in sl:
+            rr = gbr.Renderer(s.width, s.height)
+            rr.load_scene(s, CHUNK)
+            rs.append(rr)
+            b.add_scene(rr, s)
+        b.set_config(32, 2048, 6, 0)   # the autotuner's pick for these scenes
+        for _ in range(n):
+            b.render()
+        st = b.stats()
+        torch.cuda.synchronize(dev)
+        b.close()
+        for rr in rs:
+            rr.close()
+        print(json.dumps({"frames": n, "pairs": st["num_pairs"], "scenes": len(sl)}))
+        return
     if workload == "icosphere":
         import scenes
         s = scenes.icosphere_lit_scene(bin_size=16)

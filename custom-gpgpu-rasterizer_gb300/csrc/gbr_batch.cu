@@ -68,6 +68,7 @@ struct gbr_batch {
     uint32_t* d_counts = nullptr;     // kCountSplit x bins
     uint32_t* d_sub_base = nullptr;   // kCountSplit x bins
     uint32_t count_split = 1;         // sub-counters per bin in use
+    uint32_t all_flat = 0;            // every scene shades flat (the captured shade variant)
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
     ScanState* d_scan = nullptr;   // bin scan state (zeroed once)
@@ -296,6 +297,7 @@ BatchDev batch_dev(const gbr_batch* b) {
     B.items_cap = b->items_cap;
     B.num_scenes = n;
     B.phase = b->cfg.raster_phase;
+    B.all_flat = b->all_flat;
     return B;
 }
 
@@ -346,6 +348,14 @@ gbr_status render_batch(gbr_batch* b, cudaStream_t s) {
     if (st != GBR_OK) return st;
     std::vector<unsigned char> table;
     build_table(b, table);
+    // the shade pass's variant lives in the graph: a change is captured anew
+    uint32_t all_flat = 1u;
+    for (size_t i = 0; i < b->members.size(); ++i)
+        all_flat &= reinterpret_cast<const FrameDev*>(table.data())[i].flat_shade;
+    if (all_flat != b->all_flat) {
+        b->all_flat = all_flat;
+        drop_graph(b);
+    }
     if (table != b->last_table) {
         const int k = b->staging_next;
         GBR_CUDA(cudaEventSynchronize(b->staging_evt[k]));   // this staging buffer's last copy is done

@@ -241,7 +241,7 @@ struct BatchDev {
     uint32_t items_cap;
     uint32_t num_scenes;
     uint32_t phase;               // raster: triangles between hierarchical-z refreshes (0: kPhase)
-    uint32_t pad;
+    uint32_t all_flat;            // every scene shades flat: the shade pass runs its flat variant
 };
 
 // Index s of the last entry with table[s] <= v among table[0..n) (table

@@ -776,6 +776,10 @@ __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
     fill_tri(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x, (blockIdx.x * 256u + threadIdx.x) >> 5);
 }
 
+// ALL_FLAT: every scene of the batch shades flat (B.all_flat), and the
+// kernel holds only the flat path's registers (40 against 80: twice the
+// resident warps for a batch of vertex-coloured soups).
+template <bool ALL_FLAT>
 __global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {
     if (B.ctl->overflow) return;
     __shared__ __align__(16) FrameDev sF;
@@ -783,7 +787,8 @@ __global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {
     const uint32_t sc = block_scene(B, B.px_blocks, sF, s_sc);
     const uint32_t i = (blockIdx.x - __ldg(B.px_blocks + sc)) * 256u + threadIdx.x;
     if (i >= sF.width * sF.height) return;
-    if (sF.flat_shade) shade_px<true>(sF, i);
+    if (ALL_FLAT) shade_px<true>(sF, i);
+    else if (sF.flat_shade) shade_px<true>(sF, i);
     else shade_px<false>(sF, i);
 }
 
@@ -892,7 +897,10 @@ cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s
     memset(&none, 0, sizeof none);
     e = launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, raster_smem_bytes(L.bin_w, L.bin_h), s);
     if (e != cudaSuccess) return e;
-    if (L.px_blocks) batch_shade_kernel<<<L.px_blocks, 256, 0, s>>>(B);
+    if (L.px_blocks) {
+        if (B.all_flat) batch_shade_kernel<true><<<L.px_blocks, 256, 0, s>>>(B);
+        else batch_shade_kernel<false><<<L.px_blocks, 256, 0, s>>>(B);
+    }
     return cudaGetLastError();
 }
 

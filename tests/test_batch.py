@@ -101,6 +101,26 @@ def test_batch_equals_single_frames(gbr_lib, cuda_device, bin_size, chunk):
 
 
 @pytest.mark.gpu
+def test_all_flat_batch_then_textured_scene(gbr_lib, cuda_device):
+    """A batch of vertex-coloured soups runs the shade pass's flat variant;
+    switching one scene to the normal view (not flat) captures the graph
+    anew with the general variant.  Both frames equal single frames."""
+    sl = scenes.batch_scenes(6, seed=11, max_tris=30000)
+    b, rs = build_batch(gbr_lib, sl)
+    b.set_config(16, 128)
+    b.render()
+    st = b.stats()
+    assert_batch_equals_single(gbr_lib, b, sl, 16, 128)
+    sl[2].vis = scenes.VIS_NORMAL
+    b.set_view(2, sl[2].camera, sl[2].cull, sl[2].sample, sl[2].vis)
+    b.render()
+    st2 = b.stats()
+    assert st2["graph_captures"] > st["graph_captures"]
+    assert_batch_equals_single(gbr_lib, b, sl, 16, 128)
+    close_batch(b, rs)
+
+
+@pytest.mark.gpu
 def test_batch_scene_matches_oracle(gbr_lib, cuda_device):
     sl = [scenes.soup_scene(20000, 320, 240, seed=21), scenes.sphere_scene(320, 240)]
     b, rs = build_batch(gbr_lib, sl)
