@@ -641,7 +641,7 @@ def run_batch(args, rank, world, local):
     return line
 
 
-def profile_frames(n: int, binning: str = "exact", workload: str = "soup"):
+def profile_frames(n: int, binning: str = "exact", workload: str = "soup", batch_scenes: int = BATCH_SCENES):
     """The benchmark's frame, device resident, n times on the default stream
     (with the committed capacity model when binning is "predicted"); with
     workload "icosphere" the lit 4K icosphere frame with 16x16 bins."""
@@ -651,7 +651,7 @@ def profile_frames(n: int, binning: str = "exact", workload: str = "soup"):
     dev = torch.device("cuda", 0)
     if workload == "batch":
         import scenes
-        sl = scenes.batch_scenes(BATCH_SCENES, seed=0)
+        sl = scenes.batch_scenes(batch_scenes, seed=0)
         rs = []
         b = gbr.Batch()
         for s in sl:
@@ -712,6 +712,8 @@ def main():
     ap.add_argument("--workload", choices=["soup", "batch", "icosphere"], default="soup",
                     help="soup: the 1M-triangle 1080p frame; batch: 256 uneven soups as one batched frame; "
                          "icosphere: the lit 4K icosphere with 8x8 and 16x16 bins")
+    ap.add_argument("--batch-scenes", type=int, default=BATCH_SCENES,
+                    help="scenes of the batch workload (its --profile-frames too)")
     ap.add_argument("--binning", choices=["exact", "predicted"], default="exact",
                     help="binning of the --profile-frames frames")
     ap.add_argument("--profile-frames", type=int, default=0,
@@ -721,7 +723,7 @@ def main():
     if args.profile_frames:
         import build as gbr_build
         gbr_build.build()
-        profile_frames(args.profile_frames, args.binning, args.workload)
+        profile_frames(args.profile_frames, args.binning, args.workload, args.batch_scenes)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -64,7 +64,7 @@ struct gbr_batch {
     int raster_bps = 1;
 
     // device storage
-    uint32_t* d_tables = nullptr;        // tri_blocks | px_blocks | bin_base, num_scenes + 1 each
+    uint32_t* d_tables = nullptr;        // tri_blocks | px_blocks | bin_base (num_scenes + 1 each) | tri_scene | px_scene | bin_scene
     uint32_t* d_counts = nullptr;     // kCountSplit x bins
     uint32_t* d_sub_base = nullptr;   // kCountSplit x bins
     uint32_t count_split = 1;         // sub-counters per bin in use
@@ -201,6 +201,14 @@ gbr_status ensure_layout(gbr_batch* b) {
     b->total_meshes = meshes;
     b->tri_blocks = (uint32_t)tri_blocks;
     b->px_blocks = (uint32_t)px_blocks;
+    // then each triangle-pass and pixel-pass block's scene
+    tables.reserve(tables.size() + tri_blocks + px_blocks + bins);
+    for (uint32_t i = 0; i < n; ++i)
+        tables.insert(tables.end(), tables[i + 1u] - tables[i], i);
+    for (uint32_t i = 0; i < n; ++i)
+        tables.insert(tables.end(), tables[(n + 1u) + i + 1u] - tables[(n + 1u) + i], i);
+    for (uint32_t i = 0; i < n; ++i)   // and each global bin's scene
+        tables.insert(tables.end(), tables[2u * (n + 1u) + i + 1u] - tables[2u * (n + 1u) + i], i);
 
     GBR_CUDA(cudaMalloc(&b->d_tables, tables.size() * sizeof(uint32_t)));
     GBR_CUDA(cudaMemcpy(b->d_tables, tables.data(), tables.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -291,6 +299,9 @@ BatchDev batch_dev(const gbr_batch* b) {
     B.tri_blocks = b->d_tables;
     B.px_blocks = b->d_tables + (n + 1u);
     B.bin_base = b->d_tables + 2u * (n + 1u);
+    B.tri_scene = b->d_tables + 3u * (n + 1u);
+    B.px_scene = B.tri_scene + b->tri_blocks;
+    B.bin_scene = B.px_scene + b->px_blocks;
     B.items = b->d_items;
     B.ctl = b->d_ctl;
     B.list_cap = b->list_cap;

@@ -235,6 +235,9 @@ struct BatchDev {
     const uint32_t* tri_blocks;   // num_scenes + 1
     const uint32_t* px_blocks;    // num_scenes + 1
     const uint32_t* bin_base;     // num_scenes + 1
+    const uint32_t* tri_scene;    // per triangle-pass block: its scene
+    const uint32_t* px_scene;     // per pixel-pass block: its scene
+    const uint32_t* bin_scene;    // per global bin: its scene
     uint4* items;                 // (global bin, list start, count, chunks of the bin)
     Ctl* ctl;                     // the batch's list/item allocation, work queue and overflow flag
     unsigned long long list_cap;
@@ -243,17 +246,6 @@ struct BatchDev {
     uint32_t phase;               // raster: triangles between hierarchical-z refreshes (0: kPhase)
     uint32_t all_flat;            // every scene shades flat: the shade pass runs its flat variant
 };
-
-// Index s of the last entry with table[s] <= v among table[0..n) (table
-// non-decreasing, table[0] <= v).
-__device__ __forceinline__ uint32_t scene_of(const uint32_t* table, uint32_t n, uint32_t v) {
-    uint32_t lo = 0, hi = n - 1u;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1u) >> 1;
-        if (__ldg(table + mid) <= v) lo = mid; else hi = mid - 1u;
-    }
-    return lo;
-}
 
 // ---------------------------------------------------------------------------
 // Conversions with the semantics of nvcc's cvt.rzi (saturating, NaN -> 0),

@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
             cp_async_wait_all();
             uint4 it = S.item_next;
             if (BATCH && it.x != 0xFFFFFFFFu) {
-                const uint32_t sc = scene_of(B.bin_base, B.num_scenes, it.x);
+                const uint32_t sc = __ldg(B.bin_scene + it.x);
                 S.scene_next = sc;
                 it.x -= __ldg(B.bin_base + sc);
             }
@@ -750,19 +750,17 @@ __global__ void batch_reset_kernel(BatchDev B) {
 }
 
 // Block -> scene, then the scene's descriptor into shared memory.
-__device__ __forceinline__ uint32_t block_scene(const BatchDev& B, const uint32_t* table, FrameDev& sF,
-                                                uint32_t& s_sc) {
-    if (threadIdx.x == 0) s_sc = scene_of(table, B.num_scenes, blockIdx.x);
-    __syncthreads();
-    const uint32_t sc = s_sc;
+// The block's scene (from the per-block table the batch layout uploads)
+// and its frame descriptor in shared memory.
+__device__ __forceinline__ uint32_t block_scene(const BatchDev& B, const uint32_t* scene_of_block, FrameDev& sF) {
+    const uint32_t sc = __ldg(scene_of_block + blockIdx.x);
     load_scene(B, sc, sF);
     return sc;
 }
 
 __global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
     __shared__ __align__(16) FrameDev sF;
-    __shared__ uint32_t s_sc;
-    const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
+    const uint32_t sc = block_scene(B, B.tri_scene, sF);
     const uint32_t c = setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x,
                                     (blockIdx.x * 256u + threadIdx.x) >> 5);
     add_block_stats(sF.ctl, c & 0xFFFFu, c >> 16);
@@ -771,8 +769,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
 __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
     if (B.ctl->overflow) return;
     __shared__ __align__(16) FrameDev sF;
-    __shared__ uint32_t s_sc;
-    const uint32_t sc = block_scene(B, B.tri_blocks, sF, s_sc);
+    const uint32_t sc = block_scene(B, B.tri_scene, sF);
     fill_tri(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x, (blockIdx.x * 256u + threadIdx.x) >> 5);
 }
 
@@ -783,8 +780,7 @@ template <bool ALL_FLAT>
 __global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {
     if (B.ctl->overflow) return;
     __shared__ __align__(16) FrameDev sF;
-    __shared__ uint32_t s_sc;
-    const uint32_t sc = block_scene(B, B.px_blocks, sF, s_sc);
+    const uint32_t sc = block_scene(B, B.px_scene, sF);
     const uint32_t i = (blockIdx.x - __ldg(B.px_blocks + sc)) * 256u + threadIdx.x;
     if (i >= sF.width * sF.height) return;
     if (ALL_FLAT) shade_px<true>(sF, i);
