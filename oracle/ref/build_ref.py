@@ -37,6 +37,12 @@ OUT = os.path.join(ORACLE, "_ref")
 SRC = os.path.join(OUT, "src")
 REF = os.environ.get("GBR_REFERENCE_ROOT", "/root/reference")
 CCR = os.path.join(REF, "CustomCUDARasterizer")
+
+
+def reference_present() -> bool:
+    """Whether the reference's sources are on this machine (the recipe
+    builds nothing otherwise)."""
+    return os.path.isdir(CCR)
 BIN = os.path.join(OUT, "ref_harness")
 
 HOST_SOURCES = ["CUDAMesh.cpp", "CUDATexture.cpp", "CUDATextureManager.cpp", "Mesh.cpp", "SceneGraph.cpp",

@@ -1,7 +1,7 @@
 """The bin-capacity model.
 
 CPU: the float64 oracle's gradient (oracle/mlp_oracle.py) against central
-finite differences, so it can judge the GPU kernels.
+finite differences, so it can check the GPU kernels.
 GPU: the training kernels' forward and loss + gradient (BF16 parameters,
 FP32 accumulation) against the oracle; predicted-capacity binning gives bin
 lists and images identical to exact binning, both when the capacities hold
