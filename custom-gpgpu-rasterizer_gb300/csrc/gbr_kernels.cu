@@ -806,16 +806,20 @@ static uint32_t triangle_blocks(uint32_t num_tris) {
 }
 
 // Dynamic shared memory of the block-row kernels: one counter per bin (the
-// opt-in above the default 48 KB is made once per process).
+// opt-in above the default 48 KB is made once per device).
 static cudaError_t row_smem(const FrameDev& F, size_t* bytes) {
-    static bool opted = false;
+    static uint64_t opted = 0;   // bit d: done on device d (devices 0..63)
     *bytes = (size_t)F.num_bins * sizeof(uint32_t);
-    if (!opted) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (!(opted & bit)) {
         const int most = (int)(kMaxRowBins * sizeof(uint32_t));
-        cudaError_t e = cudaFuncSetAttribute(setup_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        e = cudaFuncSetAttribute(setup_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(fill_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
         if (e != cudaSuccess) return e;
-        opted = true;
+        opted |= bit;
     }
     return cudaSuccess;
 }
