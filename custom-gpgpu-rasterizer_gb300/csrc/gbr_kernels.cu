@@ -750,26 +750,48 @@ __global__ void batch_reset_kernel(BatchDev B) {
 }
 
 // Block -> scene, then the scene's descriptor into shared memory.
-// The block's scene (from the per-block table the batch layout uploads)
-// and its frame descriptor in shared memory.
-__device__ __forceinline__ uint32_t block_scene(const BatchDev& B, const uint32_t* scene_of_block, FrameDev& sF) {
-    const uint32_t sc = __ldg(scene_of_block + blockIdx.x);
+// The batch's triangle and pixel passes are cut into chunks of 256 items,
+// each belonging to one scene (B.tri_scene / B.px_scene).  A block walks a
+// contiguous range of `per` chunks and reloads its shared-memory frame
+// descriptor only when the scene changes (a scene's chunks are
+// consecutive), so the descriptor copy and its barrier are paid per scene
+// rather than per 256 items.  Walk ids stay those of the chunk (chunk * 8 +
+// warp), so the count and fill passes meet the same rank slots whatever
+// their ranges.
+__device__ __forceinline__ bool enter_scene(const BatchDev& B, uint32_t sc, uint32_t& loaded, FrameDev& sF) {
+    if (sc == loaded) return false;   // block-uniform
+    __syncthreads();                  // every thread is done with the previous descriptor
     load_scene(B, sc, sF);
-    return sc;
+    loaded = sc;
+    return true;
 }
 
-__global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B) {
+__global__ void __launch_bounds__(256) batch_setup_kernel(BatchDev B, uint32_t chunks, uint32_t per) {
     __shared__ __align__(16) FrameDev sF;
-    const uint32_t sc = block_scene(B, B.tri_scene, sF);
-    const uint32_t c = setup_tri<0>(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x,
-                                    (blockIdx.x * 256u + threadIdx.x) >> 5);
-    add_block_stats(sF.ctl, c & 0xFFFFu, c >> 16);
+    const uint32_t c0 = blockIdx.x * per, c1 = min(c0 + per, chunks);
+    uint32_t loaded = 0xFFFFFFFFu, vis = 0, fp = 0;
+    for (uint32_t v = c0; v < c1; ++v) {
+        const uint32_t sc = __ldg(B.tri_scene + v);
+        if (sc != loaded && loaded != 0xFFFFFFFFu) {   // the previous scene's statistics
+            add_block_stats(sF.ctl, vis, fp);
+            vis = fp = 0;
+        }
+        enter_scene(B, sc, loaded, sF);
+        const uint32_t c = setup_tri<0>(sF, (v - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x,
+                                        (v * 256u + threadIdx.x) >> 5);
+        vis += c & 0xFFFFu;
+        fp += c >> 16;
+    }
+    if (loaded != 0xFFFFFFFFu) add_block_stats(sF.ctl, vis, fp);
 }
 
+// The fill pass keeps one block per chunk (a range loop measured slower
+// here: 489 -> 653 us for the 256-soup batch, more registers per thread).
 __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
     if (B.ctl->overflow) return;
     __shared__ __align__(16) FrameDev sF;
-    const uint32_t sc = block_scene(B, B.tri_scene, sF);
+    const uint32_t sc = __ldg(B.tri_scene + blockIdx.x);
+    load_scene(B, sc, sF);
     fill_tri(sF, (blockIdx.x - __ldg(B.tri_blocks + sc)) * 256u + threadIdx.x, (blockIdx.x * 256u + threadIdx.x) >> 5);
 }
 
@@ -777,15 +799,20 @@ __global__ void __launch_bounds__(256) batch_fill_kernel(BatchDev B) {
 // kernel holds only the flat path's registers (40 against 80: twice the
 // resident warps for a batch of vertex-coloured soups).
 template <bool ALL_FLAT>
-__global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B) {
+__global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B, uint32_t chunks, uint32_t per) {
     if (B.ctl->overflow) return;
     __shared__ __align__(16) FrameDev sF;
-    const uint32_t sc = block_scene(B, B.px_scene, sF);
-    const uint32_t i = (blockIdx.x - __ldg(B.px_blocks + sc)) * 256u + threadIdx.x;
-    if (i >= sF.width * sF.height) return;
-    if (ALL_FLAT) shade_px<true>(sF, i);
-    else if (sF.flat_shade) shade_px<true>(sF, i);
-    else shade_px<false>(sF, i);
+    const uint32_t c0 = blockIdx.x * per, c1 = min(c0 + per, chunks);
+    uint32_t loaded = 0xFFFFFFFFu;
+    for (uint32_t v = c0; v < c1; ++v) {
+        const uint32_t sc = __ldg(B.px_scene + v);
+        enter_scene(B, sc, loaded, sF);
+        const uint32_t i = (v - __ldg(B.px_blocks + sc)) * 256u + threadIdx.x;
+        if (i >= sF.width * sF.height) continue;
+        if (ALL_FLAT) shade_px<true>(sF, i);
+        else if (sF.flat_shade) shade_px<true>(sF, i);
+        else shade_px<false>(sF, i);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -889,7 +916,13 @@ cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
 cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s) {
     if (B.num_scenes == 0) return cudaSuccess;
     batch_reset_kernel<<<(B.num_scenes + 255u) / 256u, 256, 0, s>>>(B);
-    if (L.tri_blocks) batch_setup_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
+    // chunk ranges: about 16 blocks per SM, so the ranges balance over two
+    // or more resident waves
+    const uint32_t target = 16u * (uint32_t)sm_count();
+    const uint32_t tri_per = std::max<uint32_t>(1u, (L.tri_blocks + target - 1u) / target);
+    const uint32_t px_per = std::max<uint32_t>(1u, (L.px_blocks + target - 1u) / target);
+    const uint32_t tri_grid = (L.tri_blocks + tri_per - 1u) / tri_per, px_grid = (L.px_blocks + px_per - 1u) / px_per;
+    if (L.tri_blocks) batch_setup_kernel<<<tri_grid, 256, 0, s>>>(B, L.tri_blocks, tri_per);
     cudaError_t e = launch_scan(L.scan, s);
     if (e != cudaSuccess) return e;
     if (L.tri_blocks) batch_fill_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
@@ -898,8 +931,8 @@ cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s
     e = launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, raster_smem_bytes(L.bin_w, L.bin_h), s);
     if (e != cudaSuccess) return e;
     if (L.px_blocks) {
-        if (B.all_flat) batch_shade_kernel<true><<<L.px_blocks, 256, 0, s>>>(B);
-        else batch_shade_kernel<false><<<L.px_blocks, 256, 0, s>>>(B);
+        if (B.all_flat) batch_shade_kernel<true><<<px_grid, 256, 0, s>>>(B, L.px_blocks, px_per);
+        else batch_shade_kernel<false><<<px_grid, 256, 0, s>>>(B, L.px_blocks, px_per);
     }
     return cudaGetLastError();
 }
