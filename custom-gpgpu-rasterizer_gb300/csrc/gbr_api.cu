@@ -304,6 +304,8 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
 
     const bool stages = r->timing == GBR_TIMING_STAGES;
     const bool touch = r->seen_pairs >= kListTouchMinPairs;
+    if (touch && F.row_blocks)   // the block-row count pass zeroes the last frame's entries (and 1/16 more)
+        F.touch_words = (uint32_t)((std::min<uint64_t>(r->list_cap, r->seen_pairs + r->seen_pairs / 16u) + 3u) / 4u);
     if (r->timing) GBR_CUDA(cudaEventRecord(r->ev[0], s));
     GBR_CUDA(cudaMemsetAsync(r->d_ctl, 0, sizeof(Ctl), s));
     if (predicted) {
@@ -327,7 +329,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         GBR_CUDA(launch_setup(F, false, s));
         if (stages) GBR_CUDA(cudaEventRecord(r->ev[1], s));
         GBR_CUDA(launch_scan(scan_of(F, kScanExact), s));
-        if (touch) GBR_CUDA(launch_list_touch(F, s));
+        if (touch && !F.row_blocks) GBR_CUDA(launch_list_touch(F, s));
         GBR_CUDA(launch_fill(F, s));
     }
     r->last_predicted = predicted;

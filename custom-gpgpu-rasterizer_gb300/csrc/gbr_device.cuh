@@ -168,7 +168,7 @@ struct FrameDev {
     // exact binning with block-private counter rows (row_blocks > 0)
     uint32_t* row_base;        // row_blocks x num_bins: a block's first entry in each bin it touched, bin-relative
     uint32_t row_blocks;       // blocks of the count and fill passes (0: sub-counters)
-    uint32_t row_pad;
+    uint32_t touch_words;      // block rows: 16-byte words of the list the count pass zeroes (list_touch_kernel)
     uint32_t* shade_list;      // two-pass shading: covered pixels' indices, width x height slots (null: one pass)
     uint32_t shade_pad[2];
 };

@@ -244,6 +244,12 @@ __global__ void __launch_bounds__(kRowThreads, 1) setup_rows_kernel(FrameDev F) 
         vis += c & 0xFFFFu;
         fp += c >> 16;
     }
+    // the list's first touch_words words (the last frame's entries), zeroed
+    // for the fill as list_touch_kernel does, by a pass whose memory
+    // pipeline is otherwise idle
+    uint4* const zero_to = reinterpret_cast<uint4*>(F.list);
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < F.touch_words; w += gridDim.x * blockDim.x)
+        zero_to[w] = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
     uint32_t* const row = F.row_base + (size_t)blockIdx.x * nb;
     const uint32_t shift = (uint32_t)(((unsigned long long)blockIdx.x * nb) / gridDim.x);
