@@ -280,6 +280,8 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.walk_base = r->d_walk; F.rank_next = &r->d_ctl->rank_next;
     F.ctl = r->d_ctl;
     F.scan_state = r->d_scan;
+    F.scan_spin_limit = r->scan_spin_limit;
+    F.scan_silent_tile1 = r->scan_silent_tile1;
     const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
     F.feat = r->d_feat;
     F.mlp_w = r->d_mlp_w;
@@ -347,11 +349,22 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     return GBR_OK;
 }
 
+// A bounded wait of the bin scan gave up: the frame's kernels after the scan
+// returned without touching the frame buffers.  The scan state restarts
+// from zero.
+gbr_status scan_timed_out(gbr_renderer* r) {
+    GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(r->nbx * r->nby)));
+    return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the frame is invalid");
+}
+
 // Waits for the stream; re-renders with larger bin storage if the frame
 // overflowed it.
 gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
     GBR_CUDA(cudaStreamSynchronize(s));
     GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    // a bounded wait that gave up flags the frame before any storage check
+    // (its overflow flag only stopped the kernels after the scan)
+    if (r->h_ctl->error) return scan_timed_out(r);
     for (int attempt = 0; r->h_ctl->overflow && attempt < 3; ++attempt) {
         const uint64_t need = r->h_ctl->num_pairs;
         gbr_status st = ensure_list(r, need);
@@ -361,12 +374,9 @@ gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
         if (st != GBR_OK) return st;
         GBR_CUDA(cudaStreamSynchronize(s));
         GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+        if (r->h_ctl->error) return scan_timed_out(r);
     }
     if (r->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "bin storage overflow persists");
-    if (r->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
-        GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(r->nbx * r->nby)));
-        return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the frame is invalid");
-    }
     r->seen_pairs = r->h_ctl->num_pairs;
     r->seen_visible = r->h_ctl->num_visible;
     // predicted capacities that did not fit the list: grow it for the next
@@ -638,6 +648,13 @@ gbr_status gbr_set_raster_params(gbr_renderer* r, uint32_t phase, uint32_t ctas_
         GBR_CUDA(raster_configure(r->bw, r->bh, ctas_per_sm, &bps));
         r->raster_blocks_per_sm = std::max(bps, 1);
     }
+    return GBR_OK;
+}
+
+gbr_status gbr_set_scan_wait(gbr_renderer* r, uint32_t spin_limit, int32_t silent_tile) {
+    if (!r || silent_tile < -1) return fail(GBR_ERR_INVALID_ARG, "bad renderer or silent tile %d", silent_tile);
+    r->scan_spin_limit = spin_limit;
+    r->scan_silent_tile1 = (uint32_t)(silent_tile + 1);
     return GBR_OK;
 }
 

@@ -396,6 +396,10 @@ gbr_status render_batch(gbr_batch* b, cudaStream_t s) {
 gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
     GBR_CUDA(cudaStreamSynchronize(s));
     GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    if (b->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
+        GBR_CUDA(cudaMemset(b->d_scan, 0, scan_state_bytes(b->total_bins)));
+        return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the batch frame is invalid");
+    }
     for (int attempt = 0; b->h_ctl->overflow && attempt < 3; ++attempt) {
         gbr_status st = ensure_list(b, b->h_ctl->num_pairs, b->h_ctl->items_alloc);
         if (st != GBR_OK) return st;

@@ -170,7 +170,11 @@ struct FrameDev {
     uint32_t row_blocks;       // blocks of the count and fill passes (0: sub-counters)
     uint32_t touch_words;      // block rows: 16-byte words of the list the count pass zeroes (list_touch_kernel)
     uint32_t* shade_list;      // two-pass shading: covered pixels' indices, width x height slots (null: one pass)
-    uint32_t shade_pad[2];
+    // bin-scan waits: polls of one flag before a wait gives up (0: the
+    // library's bound), and 1 + the index of a tile that publishes nothing
+    // (0: none) -- the test hook that makes a bounded wait run out
+    uint32_t scan_spin_limit;
+    uint32_t scan_silent_tile1;
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -220,6 +224,8 @@ struct ScanDev {
     uint32_t n;
     uint32_t chunk;
     uint32_t mode;
+    uint32_t spin_limit;           // polls of one flag before a look-back wait gives up (0: kScanSpinLimit)
+    uint32_t silent_tile1;         // 1 + a tile that publishes nothing (0: none; test hook)
 };
 
 // Many scenes rendered as one batch frame.  Each scene keeps its own frame

@@ -61,6 +61,8 @@ struct gbr_renderer {
     int raster_blocks_per_sm = 1;
     uint32_t raster_phase = 0;   // 0: library default
     uint32_t raster_ctas = 0;    // 0: library default
+    uint32_t scan_spin_limit = 0;     // gbr_set_scan_wait (0: the library's bound)
+    uint32_t scan_silent_tile1 = 0;   // gbr_set_scan_wait: 1 + the silent tile (0: none)
     // the last finished frame's pair and visible-triangle counts: they size
     // the next frames' raster work items and phases (0: none seen yet)
     uint64_t seen_pairs = 0, seen_visible = 0;

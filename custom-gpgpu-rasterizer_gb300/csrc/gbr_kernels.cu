@@ -195,7 +195,9 @@ template <int MODE>
 __global__ void __launch_bounds__(256) setup_kernel(FrameDev F) {
     pdl_wait();
     // predicted binning: the exact pass only runs after an overflow, and the
-    // predicted pass stops once an overflow is known
+    // predicted pass stops once an overflow is known; neither runs after a
+    // scan of the frame gave up (Ctl::overflow)
+    if (F.ctl->overflow) return;
     if (MODE == 0 ? (F.exact_guard && !F.ctl->pred_overflow) : (F.ctl->pred_overflow != 0u)) return;
     // a resident grid strides over the triangles, so that a guarded launch
     // that does not run costs one wave of early exits
@@ -235,6 +237,7 @@ __global__ void __launch_bounds__(256) fill_kernel(FrameDev F) {
 __global__ void __launch_bounds__(kRowThreads, 1) setup_rows_kernel(FrameDev F) {
     extern __shared__ uint32_t s_row[];
     pdl_wait();
+    if (F.ctl->overflow) return;
     const uint32_t nb = F.num_bins;
     for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) s_row[b] = 0u;
     __syncthreads();

@@ -23,10 +23,22 @@ namespace {
 
 constexpr uint32_t kScanSpinLimit = 1u << 22;   // polls of one flag before a wait gives up
 
-// Does this scan run at all this frame?  Exact binning behind a predicted
-// pass runs only after a predicted overflow.
+// Does this scan run at all this frame?  Not after an earlier scan of the
+// frame gave up (Ctl::overflow is set then); exact binning behind a
+// predicted pass runs only after a predicted overflow.
 __device__ __forceinline__ bool scan_runs(const ScanDev& S) {
+    if (S.ctl->overflow) return false;
     return S.mode != kScanExactAfterPredicted || S.ctl->pred_overflow != 0u;
+}
+
+// A wait that gave up, or a tile that found the state of an unfinished scan:
+// the frame's offsets cannot be trusted.  Ctl::error reports it to the host
+// (GBR_ERR_TIMEOUT); Ctl::overflow makes every later kernel of the frame
+// (fused predicted pass, guarded exact passes, fill, raster, shade) return
+// before it reads an offset, so nothing is written past the bin storage.
+__device__ __forceinline__ void give_up(Ctl* ctl) {
+    atomicOr(&ctl->error, 1u);
+    atomicExch(&ctl->overflow, 1u);
 }
 
 // Entries of bin b in the predicted modes (capacity, or filled within it).
@@ -103,7 +115,7 @@ __device__ __forceinline__ void block_scan2(unsigned long long& a, unsigned long
 // Exclusive prefix of tile `tile` (called by warp 0): 32 predecessors per
 // round, each lane waiting for one flag; the round ends at the nearest
 // published prefix (tiles before the first count as a prefix of 0).
-__device__ __forceinline__ void look_back(ScanTile* tiles, uint32_t tile, uint32_t tag, Ctl* ctl,
+__device__ __forceinline__ void look_back(ScanTile* tiles, uint32_t tile, uint32_t tag, Ctl* ctl, uint32_t limit,
                                           unsigned long long& ea, unsigned long long& eb) {
     const uint32_t lane = threadIdx.x & 31u;
     ea = 0;
@@ -117,8 +129,8 @@ __device__ __forceinline__ void look_back(ScanTile* tiles, uint32_t tile, uint32
             for (uint32_t it = 0;; ++it) {
                 f = ld_acquire(&tiles[j].flag);
                 if ((f >> 2) == tag) break;
-                if (it >= kScanSpinLimit) {
-                    atomicOr(&ctl->error, 1u);
+                if (it >= limit) {
+                    give_up(ctl);
                     f = (tag << 2) | kTilePrefix;   // give up: the frame is flagged
                     break;
                 }
@@ -154,15 +166,16 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
     __shared__ unsigned long long s_excl[2];
     __shared__ uint32_t s_tile, s_tag;
     pdl_wait();
+    if (S.mode == kScanPredictedItems && S.feat) {
+        // the pre-pass accumulators start the next frame empty (also when
+        // this frame was flagged)
+        const uint32_t n = S.n;
+        for (uint32_t b = blockIdx.x * 1024u + threadIdx.x; b < n; b += gridDim.x * 1024u)
+#pragma unroll
+            for (uint32_t k = 0; k < (uint32_t)kFeatSlots; ++k) S.feat[k * n + b] = k == 4u ? 0xFFFFFFFFu : 0u;
+    }
     if (!scan_runs(S)) return;
     if (S.mode == kScanPredictedItems) {
-        // the pre-pass accumulators start the next frame empty
-        if (S.feat) {
-            const uint32_t n = S.n;
-            for (uint32_t b = blockIdx.x * 1024u + threadIdx.x; b < n; b += gridDim.x * 1024u)
-#pragma unroll
-                for (uint32_t k = 0; k < (uint32_t)kFeatSlots; ++k) S.feat[k * n + b] = k == 4u ? 0xFFFFFFFFu : 0u;
-        }
         if (S.ctl->pred_overflow) {   // the exact pass that follows counts again
             if (blockIdx.x == 0 && threadIdx.x == 0) { S.ctl->num_visible = 0u; S.ctl->num_float_path = 0u; }
             return;
@@ -173,7 +186,7 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
         s_tag = scan_tag(ld_acquire(&S.state->seq));   // read before the ticket: the last tile bumps it
         const uint32_t t = atomicAdd(&S.state->ticket, 1u);
         if (t == ntiles - 1u) atomicExch(&S.state->ticket, 0u);   // every tile holds its ticket
-        if (t >= ntiles) atomicOr(&S.ctl->error, 1u);   // state left by a scan that did not finish
+        if (t >= ntiles) give_up(S.ctl);   // state left by a scan that did not finish
         s_tile = t;
     }
     __syncthreads();
@@ -203,12 +216,13 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
     block_scan2(ia, ib, s_a, s_b, ta, tb);
     if (threadIdx.x < 32u) {
         unsigned long long ea = 0, eb = 0;
+        const bool silent = tile + 1u == S.silent_tile1;   // test hook: this tile never publishes
         if (tile == 0) {
-            if (threadIdx.x == 0) publish_prefix(&tiles[0], ta, tb, tag);
+            if (threadIdx.x == 0 && !silent) publish_prefix(&tiles[0], ta, tb, tag);
         } else {
-            if (threadIdx.x == 0) publish_aggregate(&tiles[tile], ta, tb, tag);
-            look_back(tiles, tile, tag, S.ctl, ea, eb);
-            if (threadIdx.x == 0) publish_prefix(&tiles[tile], ea + ta, eb + tb, tag);
+            if (threadIdx.x == 0 && !silent) publish_aggregate(&tiles[tile], ta, tb, tag);
+            look_back(tiles, tile, tag, S.ctl, S.spin_limit ? S.spin_limit : kScanSpinLimit, ea, eb);
+            if (threadIdx.x == 0 && !silent) publish_prefix(&tiles[tile], ea + ta, eb + tb, tag);
         }
         if (threadIdx.x == 0) { s_excl[0] = ea; s_excl[1] = eb; }
     }
@@ -281,6 +295,8 @@ ScanDev scan_of(const FrameDev& F, uint32_t mode) {
     S.n = F.num_bins;
     S.chunk = F.chunk;
     S.mode = mode;
+    S.spin_limit = F.scan_spin_limit;
+    S.silent_tile1 = F.scan_silent_tile1;
     return S;
 }
 

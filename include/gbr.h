@@ -218,6 +218,15 @@ gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
  * phase = triangles rasterised between hierarchical-z refreshes, 0..64 (0: 16),
  * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
 gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
+/* Test hook (no counterpart in the reference, whose spin locks wait without
+ * a bound, CUDAAtomicQueue.cuh:8-26).  Every wait of the bin scan on another
+ * tile is bounded; a wait that gives up flags the frame: the kernels after
+ * the scan return without writing, and gbr_readback / gbr_get_stats /
+ * gbr_get_bins return GBR_ERR_TIMEOUT for it.  spin_limit = polls of one flag
+ * before a wait gives up (0: the library's bound, 2^22); silent_tile >= 0
+ * makes that tile of 1024 bins publish nothing, so the tiles after it wait
+ * until their bound runs out (-1: none).  Applies to the following frames. */
+gbr_status gbr_set_scan_wait(gbr_renderer *r, uint32_t spin_limit, int32_t silent_tile);
 /* Record CUDA-event times into gbr_stats (off by default).
  * GBR_TIMING_STAGES records an event between every stage, which also keeps
  * consecutive kernels from overlapping their launch; GBR_TIMING_TOTAL times
