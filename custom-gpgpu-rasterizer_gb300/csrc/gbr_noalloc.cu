@@ -29,6 +29,7 @@
 #include <mutex>
 
 #include "../../include/gbr.h"
+#include "gbr_internal.h"
 #include "gbr_kernels.h"
 
 using namespace gbr;
@@ -99,19 +100,6 @@ __global__ void noalloc_prepare_kernel(FrameDev F, MeshDev desc, uint32_t npx) {
     }
 }
 
-void mat4_mul_host(const float* lm, const float* rm, float* out) {
-    float t[16];
-    for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) {
-            float s = lm[0 * 4 + r] * rm[c * 4 + 0];
-            s = s + lm[1 * 4 + r] * rm[c * 4 + 1];
-            s = s + lm[2 * 4 + r] * rm[c * 4 + 2];
-            s = s + lm[3 * 4 + r] * rm[c * 4 + 3];
-            t[c * 4 + r] = s;
-        }
-    memcpy(out, t, sizeof t);
-}
-
 }  // namespace
 
 extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_vertices, uint32_t vertex_format,
@@ -119,7 +107,8 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
                                          const float world[16], const gbr_camera* cam, uint32_t width,
                                          uint32_t height, uint32_t num_bins_x, uint32_t num_bins_y, uint32_t bin_w,
                                          uint32_t bin_h, uint32_t queue_chunk, uint32_t cull, uint32_t sample,
-                                         uint32_t vis, uint32_t* d_colour, float* d_depth, void* stream) {
+                                         uint32_t vis, uint32_t* d_colour, float* d_depth, uint32_t* d_ids,
+                                         void* stream) {
     if (!d_vertices || !world || !cam || !d_colour || !d_depth) return na_fail(GBR_ERR_INVALID_ARG, "null argument");
     if (vertex_format > GBR_VERTEX_POS3_RGBA8 || topology > GBR_TOPOLOGY_TRIANGLE_STRIP ||
         (!d_indices && topology != GBR_TOPOLOGY_TRIANGLE_LIST) || cull > GBR_CULL_NONE || sample > GBR_SAMPLE_BILINEAR ||
@@ -168,6 +157,9 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.width = width; F.height = height;
     F.nbx = num_bins_x; F.nby = num_bins_y; F.bw = bin_w; F.bh = bin_h; F.num_bins = (uint32_t)nb;
     F.cull = cull; F.sample = sample; F.vis = vis; F.clear_colour32 = 0x003F3F3Fu;
+    // an untextured mesh in the PBR view shades from its vertex colours, as
+    // the regular entry point does (frame_basics)
+    F.flat_shade = vis == GBR_VIS_PBR ? 1u : 0u;
     F.num_meshes = 1u;
     F.num_tris = (uint32_t)tris;
     F.chunk = queue_chunk;
@@ -189,7 +181,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.list = reinterpret_cast<uint32_t*>(b + kOffList);
     F.list_cap = kNaMaxPairs;
     F.gvis = reinterpret_cast<unsigned long long*>(b + kOffGvis);
-    F.ids = reinterpret_cast<uint32_t*>(b + kOffIds);
+    F.ids = d_ids ? d_ids : reinterpret_cast<uint32_t*>(b + kOffIds);
     F.ctl = reinterpret_cast<Ctl*>(b + kOffCtl);
     F.scan_state = reinterpret_cast<ScanState*>(b + kOffScan);
     F.ranks = reinterpret_cast<uint32_t*>(b + kOffRanks);
@@ -208,8 +200,10 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     desc.num_vertices = num_vertices;
     desc.num_tris = (uint32_t)tris;
     float vp[16];
-    mat4_mul_host(cam->proj, cam->view, vp);
-    mat4_mul_host(vp, world, desc.wvp);
+    // WVP exactly as the regular entry point builds it (culling and bin
+    // rectangles depend on its rounding)
+    mat4_mul(cam->proj, cam->view, vp);
+    mat4_mul(vp, world, desc.wvp);
     memcpy(desc.world, world, sizeof desc.world);
 
     cudaStream_t s = (cudaStream_t)stream;

@@ -126,7 +126,7 @@ def lib():
             "gbr_get_bins": [vp, vp, vp, u64, C.POINTER(u64), vp],
             "gbr_get_stats": [vp, C.POINTER(Stats), vp],
             "gbr_render_noalloc": [vp, u32, u32, vp, u32, u32, vp, C.POINTER(Camera), u32, u32, u32, u32, u32, u32,
-                                   u32, u32, u32, u32, vp, vp, vp],
+                                   u32, u32, u32, u32, vp, vp, vp, vp],
             "gbr_batch_create": [C.POINTER(vp)],
             "gbr_batch_destroy": [vp],
             "gbr_batch_add": [vp, vp, C.POINTER(Camera), u32, u32, u32, C.POINTER(u32)],

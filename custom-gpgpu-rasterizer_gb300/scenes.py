@@ -317,6 +317,27 @@ def soup_scene(n: int = 1_000_000, width: int = 1920, height: int = 1080, bin_si
                  cull=cull, seed=seed)
 
 
+def strip_grid_scene(nx: int = 20, ny: int = 12, width: int = 200, height: int = 160) -> Scene:
+    """An nx x ny vertex grid (IVertex, vertex colours) drawn as one
+    triangle strip: a strip per row pair, joined by two repeated indices
+    (degenerate triangles), in the covered winding."""
+    xs, ys = np.meshgrid(np.linspace(-0.9, 0.9, nx), np.linspace(-0.8, 0.8, ny))
+    v = np.zeros(nx * ny, IVERTEX56)
+    v["p"][:, 0], v["p"][:, 1] = xs.ravel(), ys.ravel()
+    v["p"][:, 2] = 0.3 + 0.2 * np.sin(xs.ravel() * 3)
+    v["c"] = np.stack([xs.ravel() * 0.5 + 0.5, ys.ravel() * 0.5 + 0.5, np.full(nx * ny, 0.3)], -1)
+    idx = []
+    for j in range(ny - 1):
+        row = []
+        for i in range(nx):
+            row += [(j + 1) * nx + i, j * nx + i]  # counter-clockwise in NDC: the covered winding
+        if idx:
+            idx += [idx[-1], row[0]]
+        idx += row
+    m = Mesh(vertices=v, indices=np.array(idx, np.uint32), topology=TOPOLOGY_STRIP)
+    return Scene("strip", width, height, 16, 16, identity_camera(), [m], cull=CULL_NONE)
+
+
 BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1024, 768), (1920, 1080))
 
 

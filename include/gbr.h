@@ -319,8 +319,9 @@ gbr_status gbr_batch_get_bins(gbr_batch *b, uint32_t index, uint32_t *offsets, u
 
 /* No counterpart in the reference.  Renders one frame of one mesh (vertex
  * colours; no textures) from device-resident vertices into caller-owned
- * device buffers (width*height colour words and depths) without allocating
- * any device memory, for callers that may not allocate while they render:
+ * device buffers (width*height colour words and depths, and the winning
+ * primitive ids when d_ids is not NULL) without allocating any device
+ * memory, for callers that may not allocate while they render:
  * hosts with a fixed device-memory budget that forbid library allocations,
  * real-time loops that cannot take cudaMalloc's implicit synchronisation,
  * processes under a hard memory cap.  Its scratch is one static device
@@ -331,13 +332,15 @@ gbr_status gbr_batch_get_bins(gbr_batch *b, uint32_t index, uint32_t *offsets, u
  * entry count, found after the frame).  The first call on a device sets up
  * its scratch address and should come before any stream capture.  Calls
  * share the scratch: calls whose GPU work overlaps race.  Returns after
- * synchronising `stream`. */
+ * synchronising `stream`.  d_indices (NULL for a non-indexed list) stays on
+ * the device and is not range-checked: every index must be below
+ * num_vertices. */
 gbr_status gbr_render_noalloc(const void *d_vertices, uint32_t num_vertices, uint32_t vertex_format,
                               const uint32_t *d_indices, uint32_t num_indices, uint32_t topology,
                               const float world[16], const gbr_camera *cam, uint32_t width, uint32_t height,
                               uint32_t num_bins_x, uint32_t num_bins_y, uint32_t bin_w, uint32_t bin_h,
                               uint32_t queue_chunk, uint32_t cull, uint32_t sample, uint32_t vis,
-                              uint32_t *d_colour, float *d_depth, void *stream);
+                              uint32_t *d_colour, float *d_depth, uint32_t *d_ids, void *stream);
 
 const char *gbr_last_error_string(void);
 /* Library version, e.g. 0x000100 for 0.1.0. */

@@ -23,7 +23,7 @@ CUDARenderer.cu) with the staged host sources and the SDL stubs into
 oracle/_ref/ref_harness with nvcc for sm_103a, using nvcc's default
 floating-point contraction for device code (as the reference build) and
 -ffp-contract=off for host code (as MSVC, which does not fuse).
-No source under /root/reference is modified.
+No source of the reference checkout is modified.
 """
 import os
 import re
@@ -35,7 +35,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 SRC = os.path.join(OUT, "src")
-REF = os.environ.get("GBR_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: GBR_REFERENCE_ROOT, else a "reference" directory
+# beside this repository's checkout (where the build machine keeps it).
+REPO = os.path.dirname(ORACLE)
+REF = os.environ.get("GBR_REFERENCE_ROOT") or os.path.join(os.path.dirname(REPO), "reference")
 CCR = os.path.join(REF, "CustomCUDARasterizer")
 
 

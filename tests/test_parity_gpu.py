@@ -147,23 +147,7 @@ def test_multi_mesh_textured_and_vertex_coloured(gbr_lib, cuda_device):
 
 
 def strip_scene():
-    # a 20x12 grid drawn as one strip per row pair joined by degenerate triangles
-    nx, ny = 20, 12
-    xs, ys = np.meshgrid(np.linspace(-0.9, 0.9, nx), np.linspace(-0.8, 0.8, ny))
-    v = np.zeros(nx * ny, scenes.IVERTEX56)
-    v["p"][:, 0], v["p"][:, 1] = xs.ravel(), ys.ravel()
-    v["p"][:, 2] = 0.3 + 0.2 * np.sin(xs.ravel() * 3)
-    v["c"] = np.stack([xs.ravel() * 0.5 + 0.5, ys.ravel() * 0.5 + 0.5, np.full(nx * ny, 0.3)], -1)
-    idx = []
-    for j in range(ny - 1):
-        row = []
-        for i in range(nx):
-            row += [(j + 1) * nx + i, j * nx + i]  # counter-clockwise in NDC: the covered winding
-        if idx:
-            idx += [idx[-1], row[0]]
-        idx += row
-    m = scenes.Mesh(vertices=v, indices=np.array(idx, np.uint32), topology=scenes.TOPOLOGY_STRIP)
-    return scenes.Scene("strip", 200, 160, 16, 16, scenes.identity_camera(), [m], cull=scenes.CULL_NONE)
+    return scenes.strip_grid_scene()
 
 
 def test_triangle_strip(gbr_lib, cuda_device):

@@ -5,12 +5,15 @@ synchronisation, a process under a hard memory cap).  It renders from the
 caller's device buffers into the caller's device buffers and keeps its own
 scratch in one static device array, shared by every call.
 
-Checked here through the C ABI: two calls in a row, on different scenes, each
-match the regular entry point (gbr_create / gbr_render / gbr_readback)
-within the tolerance the parity tests use (colour within 1 LSB per channel,
-depth within 1e-6 relative), so nothing left in the shared scratch by the
-first call leaks into the second; and inputs beyond the scratch's limits are
-refused with an error before any GPU work.  This file is collected last so
+Checked here through the C ABI: calls in a row, on different scenes -- a
+non-indexed soup of compact vertices (two resolutions, two cull modes), the
+indexed UV sphere of 56-byte IVertex vertices, and an IVertex triangle
+strip -- each match the regular entry point (gbr_create / gbr_render /
+gbr_readback / gbr_readback_ids) within the tolerance the parity tests use
+(colour within 1 LSB per channel, depth within 1e-6 relative, winning
+primitive ids identical), so nothing left in the shared scratch by one call
+leaks into the next; and inputs beyond the scratch's limits are refused with
+an error before any GPU work.  This file is collected last so
 that a run stopping at the first failure has already run every other test.
 """
 import ctypes as C
@@ -38,6 +41,7 @@ def _noalloc(gbr, scene, torch, dev):
     npx = scene.width * scene.height
     d_col = torch.empty(npx, dtype=torch.int32, device=dev)
     d_dep = torch.empty(npx, dtype=torch.float32, device=dev)
+    d_ids = torch.empty(npx, dtype=torch.int32, device=dev)
     cam = gbr.make_camera(scene.camera)
     world = (C.c_float * 16)(*[float(x) for x in mesh.world])
     st = L.gbr_render_noalloc(C.c_void_p(d_v.data_ptr()), len(mesh.vertices), mesh.vertex_format,
@@ -45,36 +49,49 @@ def _noalloc(gbr, scene, torch, dev):
                               0 if d_ix is None else len(mesh.indices), mesh.topology, world, C.byref(cam),
                               scene.width, scene.height, scene.num_bins_x, scene.num_bins_y, scene.bin_w,
                               scene.bin_h, 256, scene.cull, scene.sample, scene.vis,
-                              C.c_void_p(d_col.data_ptr()), C.c_void_p(d_dep.data_ptr()), None)
+                              C.c_void_p(d_col.data_ptr()), C.c_void_p(d_dep.data_ptr()),
+                              C.c_void_p(d_ids.data_ptr()), None)
     assert st == 0, L.gbr_last_error_string()
     torch.cuda.synchronize(dev)
     colour = d_col.cpu().numpy().view(np.uint32).reshape(scene.height, scene.width)
     depth = d_dep.cpu().numpy().reshape(scene.height, scene.width)
-    return colour, depth
+    ids = d_ids.cpu().numpy().view(np.uint32).reshape(scene.height, scene.width)
+    return colour, depth, ids
 
 
 def _regular(gbr, scene):
     with gbr.Renderer(scene.width, scene.height) as r:
         r.load_scene(scene)
         r.render_scene(scene)
-        return r.readback()
+        colour, depth = r.readback()
+        return colour, depth, r.readback_ids()
 
 
-def _assert_close(a_colour, a_depth, b_colour, b_depth):
+def _assert_close(a, b):
+    (a_colour, a_depth, a_ids), (b_colour, b_depth, b_ids) = a, b
+    assert np.array_equal(a_ids, b_ids), f"{(a_ids != b_ids).sum()} pixels with a different winner"
     assert np.abs(_channels(a_colour) - _channels(b_colour)).max() <= 1
     za, zb = a_depth.astype(np.float64), b_depth.astype(np.float64)
     assert (np.abs(za - zb) <= 1e-6 * np.maximum(np.abs(zb), 1e-30)).all()
 
 
-def test_noalloc_matches_the_allocating_entry_point_on_two_calls_in_a_row(gbr_lib, cuda_device):
+def _untextured_sphere():
+    s = scenes.sphere_scene(640, 480)
+    for m in s.meshes:
+        m.textures = [None] * 4
+    return s
+
+
+def test_noalloc_matches_the_allocating_entry_point_on_calls_in_a_row(gbr_lib, cuda_device):
     import torch
-    first = scenes.soup_scene(20000, 512, 384, seed=31)
-    second = scenes.soup_scene(12000, 400, 300, seed=32, cull=scenes.CULL_BACKFACE)
-    for scene in (first, second):
-        colour, depth = _noalloc(gbr_lib, scene, torch, cuda_device)
-        ref_colour, ref_depth = _regular(gbr_lib, scene)
-        _assert_close(colour, depth, ref_colour, ref_depth)
-        assert (depth > 0).sum() > scene.width * scene.height // 2  # the frame is actually drawn
+    cases = [scenes.soup_scene(20000, 512, 384, seed=31),
+             scenes.soup_scene(12000, 400, 300, seed=32, cull=scenes.CULL_BACKFACE),
+             _untextured_sphere(),          # indexed triangle list, IVertex
+             scenes.strip_grid_scene()]     # indexed triangle strip, IVertex
+    for scene in cases:
+        got = _noalloc(gbr_lib, scene, torch, cuda_device)
+        _assert_close(got, _regular(gbr_lib, scene))
+        assert (got[2] != 0xFFFFFFFF).sum() > 1000  # the frame is actually drawn
 
 
 def test_noalloc_refuses_inputs_beyond_its_limits(gbr_lib, cuda_device):
@@ -87,8 +104,10 @@ def test_noalloc_refuses_inputs_beyond_its_limits(gbr_lib, cuda_device):
     cam = gbr_lib.make_camera(scenes.identity_camera())
     world = (C.c_float * 16)(*[float(x) for x in scenes.identity16()])
     st = L.gbr_render_noalloc(C.c_void_p(d_v.data_ptr()), len(big), 1, None, 0, 0, world, C.byref(cam), 64, 64,
-                              4, 4, 16, 16, 256, 2, 0, 0, C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()), None)
+                              4, 4, 16, 16, 256, 2, 0, 0, C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()), None,
+                              None)
     assert st == 1 and b"65536" in L.gbr_last_error_string()
     st = L.gbr_render_noalloc(C.c_void_p(d_v.data_ptr()), 300, 1, None, 0, 0, world, C.byref(cam), 2048, 1024,
-                              128, 64, 16, 16, 256, 2, 0, 0, C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()), None)
+                              128, 64, 16, 16, 256, 2, 0, 0, C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()), None,
+                              None)
     assert st == 1 and b"pixels" in L.gbr_last_error_string()
