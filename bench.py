@@ -246,11 +246,11 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def predicted_binning(r, scene, args, stream, flush):
+def predicted_binning(r, scene, args, stream, flush, sampled=False):
     """The same device-resident frame with learned-capacity binning (the
-    committed model): time per frame, binning time, frame overflow rate and
-    over-allocation of the predicted capacities, against exact binning on
-    the same renderer."""
+    committed model; with `sampled`, the plain sampled-count rule instead):
+    time per frame, binning time, frame overflow rate and over-allocation of
+    the predicted capacities, on the same renderer as exact binning."""
     import torch
     import gbr
     import predictor
@@ -258,7 +258,7 @@ def predicted_binning(r, scene, args, stream, flush):
     if not os.path.exists(predictor.WEIGHTS):
         return None
     sptr = stream.cuda_stream
-    predictor.install(r)
+    predictor.install(r, sampled=sampled)
     out = {"ms_per_step": [], "ms_binning": [], "overflow": 0, "over_allocation": []}
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -282,7 +282,8 @@ def predicted_binning(r, scene, args, stream, flush):
     return {"ms_per_step": t * 1e3, "triangles_per_s": N_TRI / t, "ms_binning": statistics.mean(out["ms_binning"]),
             "frame_overflow_rate": out["overflow"] / (2 * args.steps),
             "over_allocation": statistics.mean(out["over_allocation"]),
-            "model": "12-64-64-1 MLP, BF16 weights (custom-gpgpu-rasterizer_gb300/predictor_weights.npz)"}
+            "model": ("sampled pairs x 8, no network" if sampled else
+                      "12-64-64-1 MLP, BF16 weights (custom-gpgpu-rasterizer_gb300/predictor_weights.npz)")}
 
 
 def run_ours(args, rank, world, local):
@@ -355,6 +356,14 @@ def run_ours(args, rank, world, local):
     clocks = sampler.stop()
     r.set_timing(True)
     predicted = predicted_binning(r, scene, args, stream, flush)
+    if predicted is not None:
+        # learned against exact binning on the same renderer and frame
+        ms_exact = statistics.mean(ms_total)
+        bin_exact = statistics.mean(ms_setup) + statistics.mean(ms_bin)
+        predicted["frame_ratio"] = ms_exact / predicted["ms_per_step"]
+        predicted["binning_ratio"] = bin_exact / predicted["ms_binning"]
+        predicted["ms_binning_exact"] = bin_exact
+        predicted["sampled_count_rule"] = predicted_binning(r, scene, args, stream, flush, sampled=True)
     pairs = st["num_pairs"]
     t_frame = sum(ms_total) / len(ms_total) / 1e3
     (t_frame,) = max_over_ranks([t_frame], dist, dev)

@@ -135,13 +135,13 @@ void free_bins(gbr_renderer* r) {
     cudaFree(r->d_counts); cudaFree(r->d_sub_base); cudaFree(r->d_offsets); cudaFree(r->d_cursors); cudaFree(r->d_capacity);
     cudaFree(r->d_row_base);
     r->d_row_base = nullptr;
-    cudaFree(r->d_bin_done); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_scan);
+    cudaFree(r->d_bin_end); cudaFree(r->d_items); cudaFree(r->d_list); cudaFree(r->d_scan);
     r->d_scan = nullptr;
     cudaFree(r->d_feat); cudaFree(r->d_features_out);
     r->d_feat = nullptr;
     r->d_features_out = nullptr;
     r->d_sub_base = nullptr;
-    r->d_counts = r->d_offsets = r->d_cursors = r->d_capacity = r->d_bin_done = r->d_list = nullptr;
+    r->d_counts = r->d_offsets = r->d_cursors = r->d_capacity = r->d_bin_end = r->d_list = nullptr;
     r->d_items = nullptr;
     r->items_cap = 0;
     r->list_cap = 0;
@@ -273,7 +273,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.counts = r->d_counts; F.sub_base = r->d_sub_base; F.count_stride = nb; F.offsets = r->d_offsets;
     F.cursors = r->d_cursors; F.capacity = r->d_capacity;
     F.count_split = count_split_for(r->seen_pairs, nb);   // 1 until a frame has been seen
-    F.bin_done = r->d_bin_done;
+    F.bin_end = r->d_bin_end;
     F.items = r->d_items; F.items_cap = r->items_cap;
     F.list = r->d_list; F.list_cap = r->list_cap;
     F.ranks = r->d_list + r->list_cap; F.rank_cap = r->list_cap;
@@ -284,7 +284,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.scan_silent_tile1 = r->scan_silent_tile1;
     const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
     F.feat = r->d_feat;
-    F.mlp_w = r->d_mlp_w;
+    F.mlp_w = r->sampled_rule ? nullptr : r->d_mlp_w;   // null: capacities from the sampled counts alone
     F.features_out = r->collect ? r->d_features_out : nullptr;
     F.cap_alpha = r->cap_alpha; F.cap_beta = r->cap_beta; F.cap_gamma = r->cap_gamma;
     F.sample_stride = kSampleStride;
@@ -312,11 +312,19 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     GBR_CUDA(cudaMemsetAsync(r->d_ctl, 0, sizeof(Ctl), s));
     if (predicted) {
         // coarse pre-pass -> capacities -> one fused setup + fill pass; the
-        // exact kernels behind it only run if a bin overflowed
+        // exact kernels behind it only run if a bin overflowed.  The fused
+        // pass counts in block-private rows where the bins fit shared memory
+        // (its own descriptor: the guarded exact kernels behind it keep
+        // global counters).  The list is not zeroed ahead of it: the pass's
+        // own setup writes evict a zeroed region from L2 before its fill
+        // (measured: 10 us of zeroing, no gain in the fill)
+        FrameDev P = F;
+        P.touch_words = 0u;
+        if (nb <= kMaxRowBins && rows > 0u) P.row_blocks = rows;
         GBR_CUDA(launch_prepass(F, s));
         GBR_CUDA(launch_capacity(F, true, s));
         GBR_CUDA(launch_scan(scan_of(F, kScanCapacity), s));
-        GBR_CUDA(launch_setup(F, true, s));
+        GBR_CUDA(launch_setup(P, true, s));
         if (stages) GBR_CUDA(cudaEventRecord(r->ev[1], s));
         GBR_CUDA(launch_scan(scan_of(F, kScanPredictedItems), s));
         GBR_CUDA(launch_setup(F, false, s));
@@ -472,10 +480,10 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     GBR_CUDA(cudaMalloc(&r->d_cursors, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_capacity, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_capacity, 0, nb * sizeof(uint32_t)));
-    GBR_CUDA(cudaMalloc(&r->d_bin_done, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_bin_end, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_scan, scan_state_bytes(nb)));
     GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(nb)));
-    GBR_CUDA(cudaMemset(r->d_bin_done, 0, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMemset(r->d_bin_end, 0, nb * sizeof(uint32_t)));
     // pre-pass accumulators: slot 4 (depth min) starts at all ones, the rest at 0
     GBR_CUDA(cudaMalloc(&r->d_feat, (size_t)kFeatSlots * nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_feat, 0, (size_t)kFeatSlots * nb * sizeof(uint32_t)));
@@ -763,10 +771,17 @@ gbr_status gbr_get_bins(gbr_renderer* r, uint32_t* offsets, uint32_t* ids, uint6
 
 gbr_status gbr_set_predictor(gbr_renderer* r, const uint16_t* weights_bf16, uint32_t num_params, float alpha,
                              float beta, float gamma) {
-    if (!r || !weights_bf16 || num_params != (uint32_t)kMlpParams)
-        return fail(GBR_ERR_INVALID_ARG, "predictor needs %d BF16 parameters", kMlpParams);
-    if (!r->d_mlp_w) GBR_CUDA(cudaMalloc(&r->d_mlp_w, kMlpParamsPadded * sizeof(uint16_t)));
-    GBR_CUDA(cudaMemcpy(r->d_mlp_w, weights_bf16, kMlpParams * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    if (!weights_bf16 && num_params == 0u) {
+        // the plain method: l = the pre-pass's sampled pair count x the sampling stride
+        r->sampled_rule = true;
+    } else {
+        if (!weights_bf16 || num_params != (uint32_t)kMlpParams)
+            return fail(GBR_ERR_INVALID_ARG, "predictor needs %d BF16 parameters (or none)", kMlpParams);
+        if (!r->d_mlp_w) GBR_CUDA(cudaMalloc(&r->d_mlp_w, kMlpParamsPadded * sizeof(uint16_t)));
+        GBR_CUDA(cudaMemcpy(r->d_mlp_w, weights_bf16, kMlpParams * sizeof(uint16_t), cudaMemcpyHostToDevice));
+        r->sampled_rule = false;
+    }
     r->cap_alpha = alpha;
     r->cap_beta = beta;
     r->cap_gamma = gamma;

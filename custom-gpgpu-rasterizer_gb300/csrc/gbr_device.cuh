@@ -136,7 +136,7 @@ struct FrameDev {
     uint32_t* offsets;        // num_bins + 1
     uint32_t* cursors;
     uint32_t* capacity;       // predicted per-bin capacity (predicted binning)
-    uint32_t* bin_done;
+    uint32_t* bin_end;        // predicted binning: offset + capacity of each bin (the capacity scan writes it)
     uint4* items;
     uint32_t items_cap;
     uint32_t* list;
@@ -215,6 +215,7 @@ struct ScanDev {
     const uint32_t* capacity;      // predicted capacities
     uint32_t* offsets;             // n + 1
     uint32_t* cursors;
+    uint32_t* ends;                // kScanCapacity: offset + capacity of each bin
     uint4* items;
     ScanState* state;
     Ctl* ctl;

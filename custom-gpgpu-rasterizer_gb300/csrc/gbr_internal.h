@@ -71,6 +71,7 @@ struct gbr_renderer {
     uint32_t* d_feat = nullptr;
     uint16_t* d_mlp_w = nullptr;
     bool predictor_ready = false;
+    bool sampled_rule = false;   // capacities from the sampled pair counts, no network
     float cap_alpha = 0.f, cap_beta = 0.f, cap_gamma = 0.f;
     float* d_features_out = nullptr;
     bool collect = false;
@@ -92,7 +93,7 @@ struct gbr_renderer {
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
     uint32_t* d_capacity = nullptr;
-    uint32_t* d_bin_done = nullptr;
+    uint32_t* d_bin_end = nullptr;
     gbr::ScanState* d_scan = nullptr;   // bin scan state (zeroed once)
     uint4* d_items = nullptr;
     uint32_t items_cap = 0;

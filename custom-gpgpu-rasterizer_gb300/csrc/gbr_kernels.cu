@@ -288,6 +288,74 @@ __global__ void __launch_bounds__(kRowThreads, 1) fill_rows_kernel(FrameDev F) {
     pdl_release();
 }
 
+// Predicted-capacity binning on block-private counter rows, in one launch:
+// the count pass of setup_rows_kernel (setup + each pair counted in the
+// block's shared-memory row), then one run per bin the block touched,
+// reserved with a global atomic on the bin's cursor (which the capacity
+// scan set to the bin's offset) and checked against the bin's end (offset +
+// predicted capacity), then the fill pass of fill_rows_kernel over the same
+// triangles, slots handed out from shared-memory cursors.  Against exact
+// binning it saves the scan between count and fill and the second launch;
+// against one returning global atomic per pair (setup_kernel<1>) it needs
+// one per (block, bin).  A block whose run does not fit raises
+// Ctl::pred_overflow and writes nothing (the exact kernels queued behind
+// re-bin the frame); the other blocks' runs lie inside their capacities.
+__global__ void __launch_bounds__(kRowThreads, 1) predicted_rows_kernel(FrameDev F) {
+    extern __shared__ uint32_t s_row[];
+    __shared__ uint32_t s_ovf;
+    pdl_wait();
+    if (F.ctl->overflow || F.ctl->pred_overflow) return;   // block-uniform
+    const uint32_t nb = F.num_bins, tid = threadIdx.x;
+    for (uint32_t b = tid; b < nb; b += kRowThreads) s_row[b] = 0u;
+    if (tid == 0) s_ovf = 0u;
+    __syncthreads();
+    uint32_t vis = 0, fp = 0;
+    for (uint32_t base = blockIdx.x * kRowThreads; base < F.num_tris; base += gridDim.x * kRowThreads) {
+        const uint32_t c = setup_tri<2>(F, base + tid, (base + tid) >> 5, s_row);
+        vis += c & 0xFFFFu;
+        fp += c >> 16;
+    }
+    __syncthreads();
+    // one run per bin the block touched (blocks start their sweep at
+    // different bins); a thread's atomics are issued back to back
+    const uint32_t shift = (uint32_t)(((unsigned long long)blockIdx.x * nb) / gridDim.x);
+    for (uint32_t i0 = 0; i0 < nb; i0 += 8u * kRowThreads) {
+        uint32_t bb[8], cc[8], rr[8];
+#pragma unroll
+        for (uint32_t u = 0; u < 8u; ++u) {
+            const uint32_t i = i0 + u * kRowThreads + tid;
+            uint32_t b = i + shift;
+            if (b >= nb) b -= nb;
+            bb[u] = b;
+            cc[u] = i < nb ? s_row[b] : 0u;
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < 8u; ++u)
+            if (cc[u]) rr[u] = atomicAdd(&F.cursors[bb[u]], cc[u]);
+#pragma unroll
+        for (uint32_t u = 0; u < 8u; ++u) {
+            if (!cc[u]) continue;
+            if ((unsigned long long)rr[u] + cc[u] > __ldg(&F.bin_end[bb[u]])) {
+                s_ovf = 1u;
+                atomicOr(&F.ctl->pred_overflow, 1u);
+            }
+            s_row[bb[u]] = rr[u];
+        }
+    }
+    __syncthreads();
+    if (!s_ovf) {
+        for (uint32_t base = blockIdx.x * kRowThreads; base < F.num_tris; base += gridDim.x * kRowThreads) {
+            const uint32_t prim = base + tid;
+            const bool in_range = prim < F.num_tris;
+            const uint2 rect = in_range ? F.rects[prim] : empty_rect();
+            const uint32_t entry = prim | ((rect.y & 0x80000000u) ? kNoRasterBit : 0u);
+            bin_walk<5>(F, rect, entry, in_range, prim >> 5, s_row);
+        }
+    }
+    add_block_stats(F.ctl, vis, fp);
+    pdl_release();
+}
+
 // Zeros over the frame's bin-list entries [0, num_pairs) in whole 16-byte
 // words, before the exact fill pass scatters its 4-byte stores there.  The
 // list's sectors are then fully written in L2, and the scattered stores
@@ -854,6 +922,8 @@ static cudaError_t row_smem(const FrameDev& F, size_t* bytes) {
         const int most = (int)(kMaxRowBins * sizeof(uint32_t));
         e = cudaFuncSetAttribute(setup_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(fill_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(predicted_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
         if (e != cudaSuccess) return e;
         opted |= bit;
     }
@@ -861,6 +931,12 @@ static cudaError_t row_smem(const FrameDev& F, size_t* bytes) {
 }
 
 cudaError_t launch_setup(const FrameDev& F, bool predicted, cudaStream_t s) {
+    if (predicted && F.row_blocks) {
+        size_t smem = 0;
+        const cudaError_t e = row_smem(F, &smem);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(predicted_rows_kernel, dim3(F.row_blocks), dim3(kRowThreads), smem, s, F);
+    }
     if (!predicted && F.row_blocks) {
         size_t smem = 0;
         const cudaError_t e = row_smem(F, &smem);

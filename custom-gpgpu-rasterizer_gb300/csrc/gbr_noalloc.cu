@@ -88,7 +88,7 @@ __global__ void noalloc_prepare_kernel(FrameDev F, MeshDev desc, uint32_t npx) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < F.num_bins; i += stride) {
 #pragma unroll
         for (uint32_t k = 0; k < kCountSplit; ++k) F.counts[k * F.num_bins + i] = 0u;
-        F.bin_done[i] = 0u;
+        F.bin_end[i] = 0u;
     }
     // the caller's scratch: the bin scan state starts zeroed every frame
     uint32_t* scan = reinterpret_cast<uint32_t*>(F.scan_state);
@@ -175,7 +175,7 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.offsets = reinterpret_cast<uint32_t*>(b + kOffOffsets);
     F.cursors = reinterpret_cast<uint32_t*>(b + kOffCursors);
     F.capacity = reinterpret_cast<uint32_t*>(b + kOffCapacity);
-    F.bin_done = reinterpret_cast<uint32_t*>(b + kOffBinDone);
+    F.bin_end = reinterpret_cast<uint32_t*>(b + kOffBinDone);
     F.items = reinterpret_cast<uint4*>(b + kOffItems);
     F.items_cap = kNaMaxItems;
     F.list = reinterpret_cast<uint32_t*>(b + kOffList);

@@ -244,14 +244,16 @@ __device__ __forceinline__ float mlp_forward_warp(const uint16_t* w, const float
     return y + wbf(w, kOffB3);
 }
 
-// Features of every bin (and, with `predict`, the model's capacity), one
-// bin per warp, the BF16 parameters copied to shared memory once per block
-// with 16-byte loads.
+// Features of every bin (and, with `predict`, its capacity), one bin per
+// warp.  predict 1: the model, its BF16 parameters copied to shared memory
+// once per block with 16-byte loads; predict 2: no model, the predicted
+// count is the plain estimate from the pre-pass (sampled pairs x the
+// sampling stride, feature 0 x 256).
 __global__ void __launch_bounds__(256) capacity_kernel(FrameDev F, int predict) {
     __shared__ __align__(16) uint16_t w[kMlpParamsPadded];
     __shared__ float h1s[8][kMlpHidden];
     pdl_wait();
-    if (predict) {
+    if (predict == 1) {
         const uint4* src = reinterpret_cast<const uint4*>(F.mlp_w);
         uint4* dst = reinterpret_cast<uint4*>(w);
         for (int i = (int)threadIdx.x; i < kMlpParamsPadded / 8; i += (int)blockDim.x) dst[i] = __ldg(src + i);
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(256) capacity_kernel(FrameDev F, int predict) 
         if (F.features_out && lane == 0)
             for (int k = 0; k < kFeatures; ++k) F.features_out[(size_t)b * kFeatures + k] = x[k];
         if (!predict) continue;
-        const float l = softplus(mlp_forward_warp(w, x, h1s[warp]));
+        const float l = predict == 1 ? softplus(mlp_forward_warp(w, x, h1s[warp])) : x[0] * 256.f;
         if (lane != 0) continue;
         const float cap = ceilf(l * (1.f + F.cap_alpha) + F.cap_beta * sqrtf(l + 1.f) + F.cap_gamma);
         // a bin never holds more than every triangle; an undefined prediction
@@ -609,11 +611,12 @@ cudaError_t launch_prepass(const FrameDev& F, cudaStream_t s) {
 }
 
 cudaError_t launch_capacity(const FrameDev& F, bool predict, cudaStream_t s) {
-    if (predict)   // the model on the tensor cores, 128 bins per CTA
+    if (predict && F.mlp_w)   // the model on the tensor cores, 128 bins per CTA
         return launch_pdl(capacity_tc_kernel, dim3(std::max<uint32_t>((F.num_bins + 127u) / 128u, 1u)), dim3(128), 0, s, F);
-    // features only (training data): 8 warps per block, one bin per warp
+    // features only (training data), or capacities from the sampled counts:
+    // 8 warps per block, one bin per warp
     const uint32_t blocks = std::min<uint32_t>((F.num_bins + 7u) / 8u, 4096u);
-    return launch_pdl(capacity_kernel, dim3(blocks ? blocks : 1u), dim3(256), 0, s, F, 0);
+    return launch_pdl(capacity_kernel, dim3(blocks ? blocks : 1u), dim3(256), 0, s, F, predict ? 2 : 0);
 }
 
 

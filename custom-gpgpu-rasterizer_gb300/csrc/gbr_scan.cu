@@ -237,6 +237,7 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
         if (S.mode == kScanCapacity) {
             S.offsets[b] = (uint32_t)run;
             S.cursors[b] = (uint32_t)run;
+            S.ends[b] = (uint32_t)(run + c);
         } else {
             if (exact) {
                 S.offsets[b] = (uint32_t)run;
@@ -286,6 +287,7 @@ ScanDev scan_of(const FrameDev& F, uint32_t mode) {
     S.capacity = F.capacity;
     S.offsets = F.offsets;
     S.cursors = F.cursors;
+    S.ends = F.bin_end;
     S.items = F.items;
     S.state = F.scan_state;
     S.ctl = F.ctl;

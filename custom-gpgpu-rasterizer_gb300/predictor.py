@@ -240,11 +240,19 @@ def load(path=WEIGHTS):
     return d["weights_bf16"].astype(np.uint16), a, b, g, json.loads(str(d["meta"]))
 
 
-def install(renderer, path=WEIGHTS):
-    """Loads the committed model into a renderer and switches it to predicted binning."""
-    w, a, b, g, _ = load(path)
-    gbr.check(renderer._lib.gbr_set_predictor(renderer.h, w.ctypes.data_as(C.c_void_p), len(w), C.c_float(a),
-                                              C.c_float(b), C.c_float(g)))
+def install(renderer, path=WEIGHTS, sampled: bool = False):
+    """Loads the committed model into a renderer and switches it to predicted
+    binning.  With `sampled`, the method without the network instead: the
+    predicted count of a bin is its sampled pair count times the sampling
+    stride, under the capacity rule fitted for it on the same held-out bins
+    (meta "sampled_count_rule")."""
+    w, a, b, g, meta = load(path)
+    if sampled:
+        a, b, g = (float(x) for x in meta["sampled_count_rule"])
+        gbr.check(renderer._lib.gbr_set_predictor(renderer.h, None, 0, C.c_float(a), C.c_float(b), C.c_float(g)))
+    else:
+        gbr.check(renderer._lib.gbr_set_predictor(renderer.h, w.ctypes.data_as(C.c_void_p), len(w), C.c_float(a),
+                                                  C.c_float(b), C.c_float(g)))
     renderer.set_binning(gbr.BINNING_PREDICTED)
 
 
@@ -274,8 +282,11 @@ def main():
     lam = predict(w, Xv)
     alpha, beta, gamma = fit_rule(lam, yv)
     cap = capacity(lam, alpha, beta, gamma)
-    # the same rule on the plain sampled estimate (8 x sampled pairs) for comparison
-    lam0 = Xv[:, 0] * SAMPLED_SCALE
+    # the same rule on the plain sampled estimate (8 x sampled pairs) for
+    # comparison, in float64 (a float32 sum of a million capacities overflows)
+    lam0 = Xv[:, 0].astype(np.float64) * SAMPLED_SCALE
+    yv = yv.astype(np.float64)
+    lam = lam.astype(np.float64)
     a0, b0, g0 = fit_rule(lam0, yv)
     cap0 = capacity(lam0, a0, b0, g0)
     meta = {"pairs": int(len(y)), "frames": len(frames), "epochs": args.epochs, "loss": hist,
