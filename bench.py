@@ -19,6 +19,15 @@ cpu_baseline  the reference's own CPU renderer (ERenderer.cpp, built from
         full frame of the same soup; the oracle port (CPU restatement of the
         reference's GPU pipeline) on all host cores where it does not build.
 
+config  also carries, measured in the same run: predicted-capacity binning
+        of the same frame (the committed model, and the plain sampled-count
+        rule) with its frame and binning ratios against exact binning; the
+        lit 4K icosphere-7 with 8x8 and 16x16 bins ("icosphere7_4k"); the
+        256-scene batch with the autotuner's pick over bins {8, 16, 32} x
+        queue chunks {32, 64, 128} x raster variants, wider chunks as an
+        extra, and N concurrent reference ERenderers on the host cores as
+        its CPU baseline ("batch_256").  --soup-only skips the last two.
+
 --impl reference times that CPU renderer on the same workload: one full
 frame of the 1M soup per step (about 3 s on one core).
 Under torchrun each rank renders its own seeded frame (independent
@@ -417,6 +426,21 @@ def run_ours(args, rank, world, local):
     for rr in rs:
         rr.close()
 
+    # the workload's other configurations, measured in the same run and
+    # nested in this line: the lit 4K icosphere and the 256-scene batch
+    extra = {}
+    if world == 1 and not args.soup_only:
+        import copy
+        sub = copy.copy(args)
+        sub.steps, sub.warmup = min(args.steps, 10), max(3, min(args.warmup, 5))
+        ico = run_icosphere(sub, rank, world, local, nested=True)
+        extra["icosphere7_4k"] = {"metric": ico["metric"], "value": ico["value"], "unit": UNIT,
+                                  "ms_per_step": ico["ms_per_step"], "steps": sub.steps, **ico["config"]}
+        bat = run_batch(sub, rank, world, local, nested=True)
+        extra["batch_256"] = {"metric": bat["metric"], "value": bat["value"], "unit": UNIT,
+                              "ms_per_step": bat["ms_per_step"], "steps": sub.steps, "e2e": bat["e2e"],
+                              "cpu_baseline": bat["cpu_baseline"], **bat["config"]}
+
     line = None
     if rank == 0:
         cpu = None
@@ -442,7 +466,7 @@ def run_ours(args, rank, world, local):
                            "ms_setup": statistics.mean(ms_setup), "ms_bin": statistics.mean(ms_bin),
                            "ms_raster": statistics.mean(ms_raster), "ms_shade": statistics.mean(ms_shade),
                            "frame_hbm_frac": frame_bytes / t_frame / 1e9 / peak,
-                           "predicted_binning": predicted},
+                           "predicted_binning": predicted, **extra},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": profile_traffic(), "kernel": "raster_kernel",
                              "peak_source": peak_kind, "algorithmic_bytes_per_launch": raster_bytes},
@@ -460,11 +484,12 @@ def run_ours(args, rank, world, local):
     return line
 
 
-def run_icosphere(args, rank, world, local):
+def run_icosphere(args, rank, world, local, nested=False):
     """The dense sub-pixel workload: the displaced icosphere (7 subdivisions,
     327,680 triangles) at 3840x2160 with the 2048^2 noise texture, bilinear
     filtering and a directional plus a point light, with 8x8 and with 16x16
-    bins."""
+    bins.  Prints its line, or with `nested` returns it (the default run
+    nests it in the soup's line)."""
     import torch
     import gbr
     import scenes
@@ -511,36 +536,86 @@ def run_icosphere(args, rank, world, local):
     n_tri = s.num_triangles
     best = min(per_bins, key=lambda k: per_bins[k]["ms_frame"])
     t = per_bins[best]["ms_frame"] / 1e3
-    if rank == 0:
-        print(json.dumps({"metric": "triangles/s (icosphere-7 3840x2160, bilinear, directional + point light)",
-                          "value": n_tri / t, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                          "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-                          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mesh)",
-                          "config": {"workload": "icosphere7-4k-lit", "triangles": n_tri,
-                                     "resolution": [3840, 2160], "best_bins": best,
-                                     "bins_8x8": per_bins[8], "bins_16x16": per_bins[16],
-                                     "l2": "256 MB write between timed frames"},
-                          # setup, scan, fill, raster, shade queue, shade; two bin sizes
-                          "gpu_launches": 6 * args.steps * 2, "clocks": clocks}), flush=True)
+    line = {"metric": "triangles/s (icosphere-7 3840x2160, bilinear, directional + point light)",
+            "value": n_tri / t, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mesh)",
+            "config": {"workload": "icosphere7-4k-lit", "triangles": n_tri,
+                       "resolution": [3840, 2160], "best_bins": best,
+                       "bins_8x8": per_bins[8], "bins_16x16": per_bins[16],
+                       "l2": "256 MB write between timed frames"},
+            # setup, scan, fill, raster, shade queue, shade; two bin sizes
+            "gpu_launches": 6 * args.steps * 2, "clocks": clocks}
+    if rank == 0 and not nested:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 BATCH_SCENES = 256
 BATCH_METRIC = "triangles/s (256 uneven soups, one batched frame)"
 
 
-def run_batch(args, rank, world, local):
+def reference_cpu_batch(sl, workers: int, every: int = 8):
+    """The batch workload's CPU baseline: N concurrent instances of the
+    reference's ERenderer (ERenderer.cpp:42-164, single-threaded as written),
+    one scene per instance, `workers` at a time, on every `every`-th scene of
+    the batch (a bounded sample).  Each instance renders one warm-up and one
+    timed frame; the aggregate is the sample's triangles over its instances'
+    timed frame times divided among the workers that ran them concurrently.
+    None where the reference does not build here."""
+    import concurrent.futures as cf
+    try:
+        from oracle.ref import build_ref, ref_io
+        exe = build_ref.build_erenderer()
+        sample = sl[::every]
+        with tempfile.TemporaryDirectory() as d:
+            paths = []
+            for i, s in enumerate(sample):
+                p = os.path.join(d, f"scene{i}.bin")
+                ref_io.write_scene(s, p)
+                paths.append(p)
+
+            def one(p):
+                out = subprocess.run([exe, p, "1", "1"], capture_output=True, text=True, check=True)
+                return json.loads(out.stdout.strip().splitlines()[-1])
+            t0 = time.perf_counter()
+            with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+                res = list(ex.map(one, paths))
+            wall = time.perf_counter() - t0
+        tris = sum(r["triangles"] for r in res)
+        busy = sum(r["ms_per_frame"] for r in res) / 1e3
+        return {"value": tris / (busy / workers), "unit": UNIT, "cores": workers, "kind": "reference",
+                "sample": (f"{len(sample)} of the {len(sl)} scenes (every {every}th, {tris} triangles), one "
+                           f"ERenderer process per scene, {workers} at a time, one timed frame each after a "
+                           f"warm-up frame; wall {wall:.1f} s including scene loading")}
+    except Exception as e:  # noqa: BLE001 -- reported, the batch line then has no CPU baseline
+        print(f"reference CPU renderer unavailable for the batch ({type(e).__name__}: {e})", file=sys.stderr)
+        return None
+
+
+# The batch autotuner's space: the workload's bin sizes and queue chunks,
+# and the raster variants (CTAs of 256 threads per SM).  Wider chunks are
+# tuned separately and reported beside it.
+BATCH_BINS = (8, 16, 32)
+BATCH_CHUNKS = (32, 64, 128)
+BATCH_WIDE_CHUNKS = (512, 2048, 4096)
+BATCH_RASTER_CTAS = (5, 6)
+
+
+def run_batch(args, rank, world, local, nested=False, dist=None):
     """The batched workload: 256 seeded soups (1k-500k triangles, resolutions
     256^2 .. 1920x1080), one graph-replayed launch chain per batch frame, bin
     size / queue chunk / raster variant chosen by the autotuner; beside it,
-    the same scenes rendered one frame per scene on the same stream."""
+    the same scenes rendered one frame per scene on the same stream, and N
+    concurrent reference ERenderers on the host.  Prints its line, or with
+    `nested` returns it."""
     import torch
     import gbr
     import scenes
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    dist = None
-    if world > 1:
+    if world > 1 and dist is None:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     sl = scenes.batch_scenes(BATCH_SCENES, seed=rank)
@@ -557,8 +632,20 @@ def run_batch(args, rank, world, local):
     for r, s in zip(rs, sl):
         b.add_scene(r, s)
     t0 = time.perf_counter()
+    wide = None
     with torch.cuda.stream(stream):
-        best = b.autotune(bin_sizes=(8, 16, 32), chunks=(128, 512, 2048), raster_ctas=(5, 6), frames=2, stream=sptr)
+        # wider queue chunks than the workload names: tuned first, timed, reported as an extra
+        wide_cfg = b.autotune(bin_sizes=BATCH_BINS, chunks=BATCH_WIDE_CHUNKS, raster_ctas=BATCH_RASTER_CTAS, frames=2,
+                              stream=sptr)
+        b.set_timing(True)
+        ms_w = []
+        for _ in range(3):
+            flush.zero_()
+            b.render(sptr)
+            ms_w.append(b.stats(sptr)["ms_frame"])
+        wide = {"tuned": wide_cfg, "ms_frame": statistics.median(ms_w)}
+        best = b.autotune(bin_sizes=BATCH_BINS, chunks=BATCH_CHUNKS, raster_ctas=BATCH_RASTER_CTAS, frames=2,
+                          stream=sptr)
     t_tune = time.perf_counter() - t0
     b.set_timing(True)
     with torch.cuda.stream(stream):
@@ -623,6 +710,9 @@ def run_batch(args, rank, world, local):
                 e2e.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e)
     t_batch, t_e2e, t_seq = max_over_ranks([t_batch, t_e2e, t_seq], dist, dev)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = reference_cpu_batch(sl, os.cpu_count() or 1)
     line = None
     if rank == 0:
         line = {"metric": BATCH_METRIC, "value": world * n_tri / t_batch, "unit": UNIT, "n_gpus": world,
@@ -636,16 +726,20 @@ def run_batch(args, rank, world, local):
                            "per_scene_frames_ms": t_seq * 1e3,
                            "per_scene_triangles_per_s": world * n_tri / t_seq,
                            "batch_speedup_vs_per_scene": t_seq / t_batch,
+                           "autotune_space": {"bins": BATCH_BINS, "queue_chunks": BATCH_CHUNKS,
+                                              "raster_ctas": BATCH_RASTER_CTAS},
+                           "wide_chunks": wide,
                            "l2": "256 MB write between timed frames"},
                 "e2e": {"value": world * n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": 6 * args.steps,   # reset, setup, scan, fill, raster, shade
-                "clocks": clocks}
-        print(json.dumps(line), flush=True)
+                "clocks": clocks, "cpu_baseline": cpu}
+        if not nested:
+            print(json.dumps(line), flush=True)
     b.close()
     for r in rs:
         r.close()
-    if dist:
+    if dist and not nested:
         dist.barrier()
         dist.destroy_process_group()
     return line
@@ -719,6 +813,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--soup-only", action="store_true",
+                    help="the 1M-triangle soup alone (the default run also measures the icosphere and the batch)")
     ap.add_argument("--workload", choices=["soup", "batch", "icosphere"], default="soup",
                     help="soup: the 1M-triangle 1080p frame; batch: 256 uneven soups as one batched frame; "
                          "icosphere: the lit 4K icosphere with 8x8 and 16x16 bins")

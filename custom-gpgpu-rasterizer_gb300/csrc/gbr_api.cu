@@ -158,8 +158,8 @@ gbr_status ensure_list(gbr_renderer* r, uint64_t pairs) {
     cudaFree(r->d_items);
     r->d_list = nullptr;
     r->d_items = nullptr;
-    // work items of up to queue_chunk entries, as short as kMinChunk
-    const uint64_t items = (uint64_t)nb + cap / std::min(r->chunk, kMinChunk) + 1u;
+    // work items of kMinChunk..kMaxChunk entries
+    const uint64_t items = (uint64_t)nb + cap / kMinChunk + 1u;
     // the bin list, then as many rank slots (exact binning's count pass)
     if (cudaMalloc(&r->d_list, 2u * cap * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&r->d_items, items * sizeof(uint4)) != cudaSuccess) {
@@ -255,16 +255,18 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.nbx = r->nbx; F.nby = r->nby; F.bw = r->bw; F.bh = r->bh; F.num_bins = nb;
     // raster work: once a frame has been seen, items hold about half of a
     // raster CTA's share of the pairs (so a few crowded bins do not
-    // serialise the frame), within [kMinChunk, queue_chunk]; and with the
+    // serialise the frame), within [kMinChunk, kMaxChunk]; queue_chunk is
+    // the pass size (entries depth-sorted and rasterised at a time); with the
     // library's phase, triangles spanning under 4 bins on average (little
     // overdraw per bin) refresh the tile's depth bound every kMaxPhase
     // triangles rather than every kPhase
-    F.chunk = r->chunk;
+    F.chunk = kMaxChunk;
+    F.stage = r->chunk;   // queue_chunk: entries per raster pass
     F.phase = r->raster_phase;
     if (r->seen_pairs) {
         const uint64_t grid = (uint64_t)r->num_sms * (uint64_t)std::max(r->raster_blocks_per_sm, 1);
         const uint64_t share = r->seen_pairs / (2u * grid);
-        F.chunk = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(share, r->chunk), std::min(r->chunk, kMinChunk));
+        F.chunk = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(share, kMaxChunk), kMinChunk);
         if (F.phase == 0u) F.phase = r->seen_pairs < 4u * r->seen_visible ? kMaxPhase : kPhase;
     }
     F.raster_ctas = r->raster_ctas;

@@ -128,7 +128,7 @@ gbr_status ensure_list(gbr_batch* b, uint64_t pairs, uint64_t items) {
     uint64_t cap = std::max<uint64_t>(std::max<uint64_t>(pairs + pairs / 4u, b->list_cap), 1u << 20);
     if (cap > 0x7FFFFFFFull) cap = 0x7FFFFFFFull;
     if (pairs > cap) return fail(GBR_ERR_OUT_OF_MEMORY, "batch needs %llu bin entries (max 2^31-1)", (unsigned long long)pairs);
-    uint64_t icap = std::max<uint64_t>(items + items / 4u, (uint64_t)b->total_bins + cap / std::max(b->cfg.queue_chunk, 1u) + 1u);
+    uint64_t icap = std::max<uint64_t>(items + items / 4u, (uint64_t)b->total_bins + cap / kBatchChunk + 1u);
     icap = std::max<uint64_t>(icap, b->items_cap);
     if (icap > 0xFFFFFFFFull) icap = 0xFFFFFFFFull;
     drop_graph(b);
@@ -267,7 +267,8 @@ void build_table(gbr_batch* b, std::vector<unsigned char>& out) {
         FrameDev F;
         frame_basics(m.r, &m.cam, m.cull, m.sample, m.vis, F);
         F.nbx = L.nbx; F.nby = L.nby; F.bw = b->cfg.bin_size; F.bh = b->cfg.bin_size; F.num_bins = L.nbx * L.nby;
-        F.chunk = b->cfg.queue_chunk;
+        F.chunk = kBatchChunk;
+        F.stage = b->cfg.queue_chunk;
         F.phase = b->cfg.raster_phase;
         F.raster_ctas = b->cfg.raster_ctas;
         F.meshes = d_meshes + L.mesh_base;
@@ -309,6 +310,7 @@ BatchDev batch_dev(const gbr_batch* b) {
     B.num_scenes = n;
     B.phase = b->cfg.raster_phase;
     B.all_flat = b->all_flat;
+    B.stage = b->cfg.queue_chunk;
     return B;
 }
 
@@ -333,7 +335,7 @@ gbr_status capture_graph(gbr_batch* b) {
     L.scan.list_cap = b->list_cap;
     L.scan.items_cap = b->items_cap;
     L.scan.n = b->total_bins;
-    L.scan.chunk = b->cfg.queue_chunk;
+    L.scan.chunk = kBatchChunk;
     L.scan.mode = kScanExact;
     GBR_CUDA(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = launch_batch(B, L, b->cap_stream);

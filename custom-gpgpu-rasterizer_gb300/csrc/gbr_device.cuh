@@ -27,6 +27,8 @@ constexpr int kDepthBuckets = 256;                // front-to-back buckets: top 
 constexpr uint32_t kPhase = 16;                   // triangles between hierarchical-z refreshes
 constexpr uint32_t kMaxPhase = 64;                // setup records staged per phase
 constexpr uint32_t kMinChunk = 64;                // smallest raster work item the library picks
+constexpr uint32_t kMaxChunk = 4096;              // largest raster work item the library picks
+constexpr uint32_t kBatchChunk = 2048;            // raster work items of a batch frame
 // Exact binning counts each bin in `count_split` sub-counters (at most
 // kCountSplit), walk w using sub-counter w mod count_split: the crowded
 // bins' atomics (a thousand per bin across the 1M soup, several thousand at
@@ -175,6 +177,11 @@ struct FrameDev {
     // (0: none) -- the test hook that makes a bounded wait run out
     uint32_t scan_spin_limit;
     uint32_t scan_silent_tile1;
+    // raster pass size (the reference's queue size, SetupBins'
+    // queueMaxSize): a work item's entries are depth-sorted and rasterised
+    // into the tile this many at a time (0 or above kBatch: kBatch)
+    uint32_t stage;
+    uint32_t stage_pad[3];
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -252,6 +259,7 @@ struct BatchDev {
     uint32_t num_scenes;
     uint32_t phase;               // raster: triangles between hierarchical-z refreshes (0: kPhase)
     uint32_t all_flat;            // every scene shades flat: the shade pass runs its flat variant
+    uint32_t stage;               // raster pass size (FrameDev::stage)
 };
 
 // ---------------------------------------------------------------------------

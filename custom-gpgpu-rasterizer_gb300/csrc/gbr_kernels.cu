@@ -537,6 +537,8 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
     const uint32_t num_items = Q->num_items;
     const uint32_t phase_req = BATCH ? B.phase : F.phase;
     const uint32_t phase = phase_req == 0u ? kPhase : min(phase_req, kMaxPhase);
+    const uint32_t stage_req = BATCH ? B.stage : F.stage;
+    const uint32_t pass = stage_req == 0u ? kBatch : min(stage_req, kBatch);   // entries per raster pass
     if (BATCH && tid == 0) S.scene_loaded = 0xFFFFFFFFu;
     // thread 0 runs one item ahead: the next item's queue slot is taken when
     // an item starts and its descriptor copied to shared memory
@@ -583,13 +585,13 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
         for (int i = (int)tid; i < npx; i += kRasterThreads) tile[i] = kEmptyVis;
         if (tid == 0) fetch_item(&S.item_next, items, next_idx, num_items);
         const uint32_t* const keys = G.keys;
-        for (uint32_t b0 = 0; b0 < count && npx > 0; b0 += kBatch) {
+        for (uint32_t b0 = 0; b0 < count && npx > 0; b0 += pass) {
             // stage the entries with their depth-key bounds (no setup record
             // is read before a triangle's phase comes) and count the
             // rasterisable ones per depth bucket
             constexpr uint32_t kPer = kBatch / kRasterThreads;
             static_assert(kDepthBuckets == kRasterThreads, "one bucket per thread");
-            const uint32_t n = min((uint32_t)kBatch, count - b0);
+            const uint32_t n = min(pass, count - b0);
             __syncthreads();   // the previous batch is done with the shared arrays
             S.bucket[tid] = 0u;
             __syncthreads();

@@ -162,7 +162,8 @@ extern "C" gbr_status gbr_render_noalloc(const void* d_vertices, uint32_t num_ve
     F.flat_shade = vis == GBR_VIS_PBR ? 1u : 0u;
     F.num_meshes = 1u;
     F.num_tris = (uint32_t)tris;
-    F.chunk = queue_chunk;
+    F.chunk = kMaxChunk;      // work items: the library's split
+    F.stage = queue_chunk;    // entries per raster pass
     for (int k = 0; k < 3; ++k) { F.cam_pos[k] = cam->pos[k]; F.cam_fwd[k] = cam->fwd[k]; }
     F.meshes = reinterpret_cast<const MeshDev*>(b + kOffMesh);
     F.setup = reinterpret_cast<TriSetup*>(b + kOffSetup);

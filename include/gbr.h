@@ -88,8 +88,11 @@ gbr_status gbr_create(uint32_t width, uint32_t height, gbr_renderer **out);
 gbr_status gbr_destroy(gbr_renderer *r);
 
 /* SetupBins(numBins, binDim, queueMaxSize) (CUDARenderer.cu:199-204).
- * queue_chunk replaces the fixed queue capacity: bins are exact-sized, and
- * a bin's list is rasterised in chunks of at most queue_chunk triangles. */
+ * Bins are exact-sized (no capacity, no dropped triangles); queue_chunk
+ * keeps the queue size's role in the raster: a bin's triangles are
+ * depth-sorted and rasterised into its tile queue_chunk at a time (at most
+ * 2048; 0 = 4096, i.e. 2048).  Long bins are split across raster CTAs by the
+ * library, in work items of 64..4096 entries sized from the last frame. */
 gbr_status gbr_setup_bins(gbr_renderer *r, uint32_t num_bins_x, uint32_t num_bins_y,
                           uint32_t bin_w, uint32_t bin_h, uint32_t queue_chunk);
 
@@ -271,7 +274,8 @@ gbr_status gbr_get_stats(gbr_renderer *r, gbr_stats *out, void *stream);
 typedef struct gbr_batch gbr_batch;
 typedef struct {
     uint32_t bin_size;     /* bins of bin_size x bin_size pixels, 1..64 */
-    uint32_t queue_chunk;  /* bin-list entries per raster work item, >= 1 */
+    uint32_t queue_chunk;  /* entries depth-sorted and rasterised per pass over a tile, >= 1 (at most 2048
+                              used); work items hold 2048 entries */
     uint32_t raster_ctas;  /* raster variant: CTAs per SM, 2..6 (0: 6) */
     uint32_t raster_phase; /* triangles between hierarchical-z refreshes, 0..64 (0: 16) */
 } gbr_batch_config;

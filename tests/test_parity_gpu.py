@@ -23,10 +23,13 @@ EMPTY = 0xFFFFFFFF
 DEPTH_RTOL = 1e-6
 
 
-def gpu_render(gbr, scene, chunk=256, renderer=None, binning=0):
+def gpu_render(gbr, scene, chunk=256, renderer=None, binning=0, frames=1):
     r = renderer or gbr.Renderer(scene.width, scene.height)
     r.load_scene(scene, chunk)
     r.set_binning(binning)
+    for _ in range(frames - 1):   # earlier frames size the work items of the last one
+        r.render_scene(scene)
+        r.stats()
     r.render_scene(scene)
     colour, depth = r.readback()
     ids = r.readback_ids()
@@ -83,8 +86,8 @@ def check_reference_band(scene, g, o, limit=400):
     return len(diff)
 
 
-def run_case(gbr, scene, chunk=256, ref_band=True):
-    g = gpu_render(gbr, scene, chunk)
+def run_case(gbr, scene, chunk=256, ref_band=True, frames=1):
+    g = gpu_render(gbr, scene, chunk, frames=frames)
     ofx = oracle.render(scene, oracle.RASTER_FIXED)
     assert_bins_equal(g, ofx)
     assert_matches_fixed(g, ofx)
@@ -125,7 +128,11 @@ def test_soup_bin_geometries(gbr_lib, cuda_device, bw, bh, w, h):
 
 @pytest.mark.parametrize("chunk", [1, 16, 100])
 def test_multi_chunk_bins_merge(gbr_lib, cuda_device, chunk):
-    g, _ = run_case(gbr_lib, scenes.soup_scene(20000, 256, 192, seed=14), chunk=chunk, ref_band=False)
+    """queue_chunk = 1, 16 or 100 entries per raster pass over a tile; on
+    the second frame the library splits bins of more than 64 entries into
+    several work items (sized from the first frame's pairs), whose tiles
+    merge in the frame buffer through 64-bit atomicMin."""
+    g, _ = run_case(gbr_lib, scenes.soup_scene(20000, 256, 192, seed=14), chunk=chunk, ref_band=False, frames=2)
     assert g["stats"]["num_work_items"] > 16 * 12
 
 
