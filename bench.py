@@ -305,7 +305,10 @@ def run_ours(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    scene = make_scene(rank)
+    # replicas: one seeded frame per rank (weak scaling); rows: one frame
+    # split across the ranks by bin rows (strong scaling, composited once)
+    split_rows = world > 1 and args.split == "rows"
+    scene = make_scene(0 if split_rows else rank)
     mesh = scene.meshes[0]
     vbytes = mesh.vertices.nbytes
     nv = len(mesh.vertices)
@@ -317,6 +320,11 @@ def run_ours(args, rank, world, local):
     r = gbr.Renderer(WIDTH, HEIGHT)
     r.setup_bins(scene.num_bins_x, scene.num_bins_y, BIN, BIN, CHUNK)
     r.bind_mesh_device(d_vert.data_ptr(), nv, mesh.vertex_format)
+    band = None
+    if split_rows:
+        import sharding
+        band = sharding.row_bands(scene.num_bins_y, world)[rank]
+        r.set_bin_rows(*band)
     r.set_timing(True)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     with torch.cuda.stream(stream):
@@ -376,7 +384,17 @@ def run_ours(args, rank, world, local):
     pairs = st["num_pairs"]
     t_frame = sum(ms_total) / len(ms_total) / 1e3
     (t_frame,) = max_over_ranks([t_frame], dist, dev)
-    value = world * N_TRI / t_frame
+    value = (1 if split_rows else world) * N_TRI / t_frame
+    composite_ok = None
+    if split_rows:   # the bands gathered into the frame once, against a one-GPU render of it
+        import sharding
+        colour, _ = r.readback(stream=sptr)
+        y0, y1 = sharding.band_pixel_rows(band, BIN, HEIGHT)
+        frame = sharding.gather_composite(dist, np.ascontiguousarray(colour[y0:y1]), y0, y1, HEIGHT, WIDTH)
+        r.set_bin_rows(0, 0)
+        r.render_scene(scene, sptr)
+        whole, _ = r.readback(stream=sptr)
+        composite_ok = bool(np.array_equal(frame, whole))
     t_raster = sum(ms_raster) / len(ms_raster) / 1e3
     raster_bytes = 4 * pairs + 8 * WIDTH * HEIGHT
     frame_bytes = vbytes + 8 * pairs + 8 * WIDTH * HEIGHT
@@ -457,16 +475,19 @@ def run_ours(args, rank, world, local):
                 cpu = {"value": N_TRI / dt, "unit": UNIT, "cores": threads, "kind": "port",
                        "sample": "one full frame of the same 1M soup (setup, binning, raster, shading)"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": t_frame * 1e3, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded soup per rank)",
+                "warmup": args.warmup, "ms_per_step": t_frame * 1e3, "higher_is_better": True,
+                "scaling": "strong" if split_rows else "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (one seeded soup split by bin rows)" if split_rows else "synthetic (seeded soup per rank)",
                 "config": {"workload": WORKLOAD, "triangles": N_TRI, "resolution": [WIDTH, HEIGHT],
                            "bins": [BIN, BIN], "queue_chunk": CHUNK, "binning": "exact two-pass",
                            "l2": "256 MB write between timed frames", "pairs": int(pairs),
-                           "frames_per_s": world / t_frame,
+                           "frames_per_s": (1 if split_rows else world) / t_frame,
                            "ms_setup": statistics.mean(ms_setup), "ms_bin": statistics.mean(ms_bin),
                            "ms_raster": statistics.mean(ms_raster), "ms_shade": statistics.mean(ms_shade),
                            "frame_hbm_frac": frame_bytes / t_frame / 1e9 / peak,
-                           "predicted_binning": predicted, **extra},
+                           "predicted_binning": predicted, **extra,
+                           "split": ({"bin_rows": list(band), "composite_equals_one_gpu_frame": composite_ok}
+                                     if split_rows else "replicas")},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": profile_traffic(), "kernel": "raster_kernel",
                              "peak_source": peak_kind, "algorithmic_bytes_per_launch": raster_bytes},
@@ -618,8 +639,14 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
     if world > 1 and dist is None:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    sl = scenes.batch_scenes(BATCH_SCENES, seed=rank)
-    n_tri = sum(s.num_triangles for s in sl)
+    # one batch of scenes for the whole job; under torchrun each rank takes
+    # its share by estimated cost (sharding.scene_partition, no collective)
+    import sharding
+    nscenes = getattr(args, "batch_scenes", BATCH_SCENES)
+    specs = scenes.batch_scene_specs(nscenes, seed=0)
+    part = sharding.scene_partition([sharding.scene_cost(n, w, h) for n, w, h, _ in specs], world)[rank]
+    sl = scenes.batch_scenes(nscenes, seed=0, only=part)
+    n_tri = sum(n for n, _, _, _ in specs)   # the job's triangles, all ranks
     stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
@@ -715,22 +742,24 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
         cpu = reference_cpu_batch(sl, os.cpu_count() or 1)
     line = None
     if rank == 0:
-        line = {"metric": BATCH_METRIC, "value": world * n_tri / t_batch, "unit": UNIT, "n_gpus": world,
+        line = {"metric": BATCH_METRIC, "value": n_tri / t_batch, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded soups per rank)",
-                "config": {"workload": "batch-256-uneven-soups", "scenes": BATCH_SCENES, "triangles": n_tri,
-                           "pixels": int(sum(s.width * s.height for s in sl)), "tuned": best,
+                "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded soups, partitioned across ranks by cost)",
+                "config": {"workload": "batch-256-uneven-soups", "scenes": nscenes, "triangles": n_tri,
+                           "scenes_per_rank": len(part),
+                           "pixels": int(sum(w * h for _, w, h, _ in specs)), "tuned": best,
                            "autotune_s": t_tune, "pairs": int(st["num_pairs"]),
                            "work_items": int(st["num_work_items"]), "graph_captures": int(st["graph_captures"]),
                            "batch_frames_per_s": 1.0 / t_batch,
                            "per_scene_frames_ms": t_seq * 1e3,
-                           "per_scene_triangles_per_s": world * n_tri / t_seq,
+                           "per_scene_triangles_per_s": n_tri / t_seq,
                            "batch_speedup_vs_per_scene": t_seq / t_batch,
                            "autotune_space": {"bins": BATCH_BINS, "queue_chunks": BATCH_CHUNKS,
                                               "raster_ctas": BATCH_RASTER_CTAS},
                            "wide_chunks": wide,
                            "l2": "256 MB write between timed frames"},
-                "e2e": {"value": world * n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "e2e": {"value": n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": 6 * args.steps,   # reset, setup, scan, fill, raster, shade
                 "clocks": clocks, "cpu_baseline": cpu}
@@ -813,6 +842,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--split", choices=["replicas", "rows"], default="replicas",
+                    help="under torchrun: one seeded soup per rank (replicas), or one soup split by bin rows")
     ap.add_argument("--soup-only", action="store_true",
                     help="the 1M-triangle soup alone (the default run also measures the icosphere and the batch)")
     ap.add_argument("--workload", choices=["soup", "batch", "icosphere"], default="soup",

@@ -283,6 +283,12 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.ctl = r->d_ctl;
     F.scan_state = r->d_scan;
     F.scan_spin_limit = r->scan_spin_limit;
+    if (r->row1) {   // this renderer's share of a frame split by bin rows
+        F.row0 = r->row0;
+        F.row1 = std::min(r->row1, r->nby);
+        F.px_begin = (F.row0 * r->bh * r->W) & ~3u;   // a multiple of 4: the quad-wide shade pass
+        F.px_end = std::min(F.row1 * r->bh, r->H) * r->W;
+    }
     F.scan_silent_tile1 = r->scan_silent_tile1;
     const bool predicted = r->binning == GBR_BINNING_PREDICTED && r->predictor_ready && !r->collect;
     F.feat = r->d_feat;
@@ -471,6 +477,7 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     cudaDeviceSynchronize();
     free_bins(r);
     r->nbx = num_bins_x; r->nby = num_bins_y; r->bw = bin_w; r->bh = bin_h; r->chunk = queue_chunk;
+    r->row0 = r->row1 = 0u;   // a new bin grid: every row
     const uint32_t nb = num_bins_x * num_bins_y;
     GBR_CUDA(cudaMalloc(&r->d_counts, (size_t)kCountSplit * nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_counts, 0, (size_t)kCountSplit * nb * sizeof(uint32_t)));
@@ -658,6 +665,16 @@ gbr_status gbr_set_raster_params(gbr_renderer* r, uint32_t phase, uint32_t ctas_
         GBR_CUDA(raster_configure(r->bw, r->bh, ctas_per_sm, &bps));
         r->raster_blocks_per_sm = std::max(bps, 1);
     }
+    return GBR_OK;
+}
+
+gbr_status gbr_set_bin_rows(gbr_renderer* r, uint32_t row0, uint32_t row1) {
+    if (!r) return fail(GBR_ERR_INVALID_ARG, "renderer is null");
+    if (!r->bins_ready) return fail(GBR_ERR_INVALID_ARG, "gbr_setup_bins was not called");
+    if (!(row0 == 0u && row1 == 0u) && !(row0 < row1 && row1 <= r->nby))
+        return fail(GBR_ERR_INVALID_ARG, "bin rows [%u, %u) outside [0, %u)", row0, row1, r->nby);
+    r->row0 = row0;
+    r->row1 = row1;
     return GBR_OK;
 }
 

@@ -181,7 +181,12 @@ struct FrameDev {
     // queueMaxSize): a work item's entries are depth-sorted and rasterised
     // into the tile this many at a time (0 or above kBatch: kBatch)
     uint32_t stage;
-    uint32_t stage_pad[3];
+    // a frame split across GPUs by bin rows: this frame bins and
+    // rasterises bin rows [row0, row1) and shades pixels [px_begin, px_end)
+    // (row1 = 0: every row; px_end = 0: every pixel)
+    uint32_t row0, row1;
+    uint32_t px_begin, px_end;
+    uint32_t rows_pad[3];
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -390,6 +395,10 @@ __device__ __forceinline__ int4 bin_rect(float2 s0, float2 s1, float2 s2, const 
     r.y = clampi(ymin / (int)F.bh, 0, (int)F.nby);
     r.z = clampi(xmax / (int)F.bw, 0, (int)F.nbx - 1);
     r.w = clampi(ymax / (int)F.bh, 0, (int)F.nby - 1);
+    if (F.row1) {   // a frame split by bin rows keeps this GPU's rows (empty if none)
+        r.y = max(r.y, (int)F.row0);
+        r.w = min(r.w, (int)F.row1 - 1);
+    }
     return r;
 }
 

@@ -711,8 +711,8 @@ __device__ __forceinline__ void shade_px(const FrameDev& F, uint32_t i) {
 template <bool FLAT>
 __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
     pdl_wait();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= F.width * F.height || F.ctl->overflow) return;
+    const uint32_t i = F.px_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (F.px_end ? F.px_end : F.width * F.height) || F.ctl->overflow) return;
     shade_px<FLAT>(F, i);
 }
 
@@ -732,8 +732,9 @@ __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
 __global__ void __launch_bounds__(256) shade_queue_kernel(FrameDev F) {
     pdl_wait();
     if (F.ctl->overflow) return;
-    const uint32_t n = F.width * F.height, lane = threadIdx.x & 31u;
-    const uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+    // pixels [px_begin, px_end) (px_begin a multiple of 4)
+    const uint32_t n = F.px_end ? F.px_end : F.width * F.height, lane = threadIdx.x & 31u;
+    const uint32_t i0 = F.px_begin + (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
     const bool aligned = ((reinterpret_cast<uintptr_t>(F.gvis) | reinterpret_cast<uintptr_t>(F.colour) |
                            reinterpret_cast<uintptr_t>(F.depth) | reinterpret_cast<uintptr_t>(F.ids)) & 15u) == 0u;
     uint32_t covered = 0;   // bit k: pixel i0 + k has a winner
@@ -983,7 +984,7 @@ cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
 }
 
 cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
-    const uint32_t npx = F.width * F.height;
+    const uint32_t npx = (F.px_end ? F.px_end : F.width * F.height) - F.px_begin;
     const dim3 g((npx + 255u) / 256u), b(256);
     if (!F.flat_shade && F.shade_list) {
         const cudaError_t e = launch_pdl(shade_queue_kernel, dim3((npx + 1023u) / 1024u), b, 0, s, F);

@@ -341,19 +341,32 @@ def strip_grid_scene(nx: int = 20, ny: int = 12, width: int = 200, height: int =
 BATCH_RESOLUTIONS = ((256, 256), (512, 512), (1024, 768), (1920, 1080))
 
 
+def batch_scene_specs(n: int = 256, seed: int = 0, min_tris: int = 1000, max_tris: int = 500_000,
+                      resolutions=BATCH_RESOLUTIONS) -> list:
+    """(triangles, width, height, seed) of each scene of batch_scenes, without
+    generating any vertex."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        count = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
+        w, h = resolutions[int(rng.integers(0, len(resolutions)))]
+        out.append((count, w, h, int(rng.integers(1 << 31))))
+    return out
+
+
 def batch_scenes(n: int = 256, seed: int = 0, min_tris: int = 1000, max_tris: int = 500_000,
-                 bin_size: int = 16, resolutions=BATCH_RESOLUTIONS) -> list:
+                 bin_size: int = 16, resolutions=BATCH_RESOLUTIONS, only=None) -> list:
     """Uneven batch of soups: scene i has a triangle count log-uniform in
     [min_tris, max_tris] and a resolution drawn from `resolutions`; each is
     drawn like the 1M soup (uniform centroids plus a 20% Gaussian blob of
     sigma 100 px, area log-uniform in 0.5-4096 px^2, random winding, depth
-    uniform in [0.1, 100], RGBA8 colours), seeded by (seed, i)."""
-    rng = np.random.default_rng(seed)
+    uniform in [0.1, 100], RGBA8 colours), seeded by (seed, i).  `only`: the
+    indices of the scenes to build (a rank's share of a partitioned batch)."""
+    specs = batch_scene_specs(n, seed, min_tris, max_tris, resolutions)
     out = []
-    for i in range(n):
-        count = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
-        w, h = resolutions[int(rng.integers(0, len(resolutions)))]
-        s = soup_scene(count, w, h, bin_size, seed=int(rng.integers(1 << 31)))
+    for i in (range(n) if only is None else only):
+        count, w, h, sseed = specs[i]
+        s = soup_scene(count, w, h, bin_size, seed=sseed)
         s.name = f"batch{i}_soup{count}_{w}x{h}"
         out.append(s)
     return out

@@ -221,6 +221,15 @@ gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
  * phase = triangles rasterised between hierarchical-z refreshes, 0..64 (0: 16),
  * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
 gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
+/* A frame split across GPUs by bin rows (no counterpart in the reference,
+ * which renders on one GPU, main.cpp:397-399): the following frames of this
+ * renderer bin and rasterise only bin rows [row0, row1) -- triangles are set
+ * up and binned as usual, their bin rectangles cut to those rows -- and shade
+ * only the pixels of those rows; pixels of other rows are left as they were.
+ * Each GPU renders its rows of the same scene and the rows are composited
+ * (the bands are disjoint, so the composite equals the one-GPU frame).
+ * (0, 0) restores every row; gbr_setup_bins also does. */
+gbr_status gbr_set_bin_rows(gbr_renderer *r, uint32_t row0, uint32_t row1);
 /* Test hook (no counterpart in the reference, whose spin locks wait without
  * a bound, CUDAAtomicQueue.cuh:8-26).  Every wait of the bin scan on another
  * tile is bounded; a wait that gives up flags the frame: the kernels after

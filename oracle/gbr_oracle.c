@@ -834,6 +834,10 @@ static void *raster_worker(void *arg)
         const int b = __sync_fetch_and_add(&job->next, 1);
         if ((uint32_t)b >= job->nbins) break;
         if ((uint32_t)b % stride != phase) continue;
+        if (job->f->bin_row1) {   /* a band of bin rows */
+            const uint32_t row = (uint32_t)b / job->f->num_bins_x;
+            if (row < job->f->bin_row0 || row >= job->f->bin_row1) continue;
+        }
         raster_bin(job, (uint32_t)b, &frags, &cov);
     }
     pthread_mutex_lock(&job->lock);

@@ -60,6 +60,8 @@ typedef struct {
     float proj[16];
     uint32_t num_lights;    /* 0: the reference shader's constant light */
     orc_light lights[ORC_MAX_LIGHTS];
+    uint32_t bin_row0;      /* rasterise only bin rows [bin_row0, bin_row1) (bin_row1 0: all): one */
+    uint32_t bin_row1;      /* GPU's band of a frame split across GPUs by bin rows */
 } orc_frame;
 
 typedef struct {

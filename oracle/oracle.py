@@ -32,7 +32,8 @@ class OrcFrame(C.Structure):
                 ("bin_stride", C.c_uint32), ("bin_phase", C.c_uint32),
                 ("cam_pos", C.c_float * 3), ("cam_fwd", C.c_float * 3),
                 ("view", C.c_float * 16), ("proj", C.c_float * 16),
-                ("num_lights", C.c_uint32), ("lights", OrcLight * MAX_LIGHTS)]
+                ("num_lights", C.c_uint32), ("lights", OrcLight * MAX_LIGHTS),
+                ("bin_row0", C.c_uint32), ("bin_row1", C.c_uint32)]
 
 
 class OrcMesh(C.Structure):
@@ -82,7 +83,8 @@ def _fptr(a: np.ndarray):
 class _Prepared:
     """Keeps the numpy buffers alive while the C structs point at them."""
 
-    def __init__(self, scene, raster_mode: int, num_threads: int, bin_stride: int = 0, bin_phase: int = 0):
+    def __init__(self, scene, raster_mode: int, num_threads: int, bin_stride: int = 0, bin_phase: int = 0,
+                 bin_rows=(0, 0)):
         f = OrcFrame()
         f.width, f.height = scene.width, scene.height
         f.num_bins_x, f.num_bins_y = scene.num_bins_x, scene.num_bins_y
@@ -92,6 +94,7 @@ class _Prepared:
         f.clear_colour32 = 0x003F3F3F
         f.num_threads = num_threads
         f.bin_stride, f.bin_phase = bin_stride, bin_phase
+        f.bin_row0, f.bin_row1 = bin_rows
         cam = scene.camera
         f.cam_pos[:] = [float(x) for x in cam.pos]
         f.cam_fwd[:] = [float(x) for x in cam.fwd]
@@ -136,14 +139,16 @@ class _Prepared:
 
 
 def render(scene, raster_mode: int = RASTER_FIXED, num_threads: int = 0, want_bins: bool = True,
-           want_image: bool = True, bin_stride: int = 0, bin_phase: int = 0):
+           want_image: bool = True, bin_stride: int = 0, bin_phase: int = 0, bin_rows=(0, 0)):
     """Render one frame; returns dict(colour, depth, ids, offsets, bins, stats).
     bin_stride > 1 rasterises only bins b with b % bin_stride == bin_phase;
+    bin_rows = (r0, r1) only bin rows [r0, r1) (one GPU's band of a frame
+    split by bin rows; pixels of other rows are the clear colour);
     want_image=False runs the vertex stage and binning only."""
     L = lib()
     if num_threads <= 0:
         num_threads = os.cpu_count() or 1
-    P = _Prepared(scene, raster_mode, num_threads, bin_stride, bin_phase)
+    P = _Prepared(scene, raster_mode, num_threads, bin_stride, bin_phase, bin_rows)
     n = scene.width * scene.height
     colour = np.empty(n, np.uint32)
     depth = np.empty(n, np.float32)
