@@ -343,6 +343,16 @@ def run_ours(args, rank, world, local):
             st = r.stats(sptr)
             ms_setup.append(st["ms_setup"]); ms_bin.append(st["ms_bin"])
             ms_raster.append(st["ms_raster"]); ms_shade.append(st["ms_shade"])
+    # the raster with setup records staged by bulk asynchronous copies
+    # (GBR_STAGING_TMA) on the same frames, for comparison
+    ms_raster_tma = []
+    r.set_raster_staging(True)
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            r.render_scene(scene, sptr)
+            ms_raster_tma.append(r.stats(sptr)["ms_raster"])
+    r.set_raster_staging(False)
     # the timed frames: frame events only
     r.set_timing(True, total_only=True)
     with torch.cuda.stream(stream):
@@ -484,6 +494,7 @@ def run_ours(args, rank, world, local):
                            "frames_per_s": (1 if split_rows else world) / t_frame,
                            "ms_setup": statistics.mean(ms_setup), "ms_bin": statistics.mean(ms_bin),
                            "ms_raster": statistics.mean(ms_raster), "ms_shade": statistics.mean(ms_shade),
+                           "ms_raster_tma_staging": statistics.mean(ms_raster_tma),
                            "frame_hbm_frac": frame_bytes / t_frame / 1e9 / peak,
                            "predicted_binning": predicted, **extra,
                            "split": ({"bin_rows": list(band), "composite_equals_one_gpu_frame": composite_ok}

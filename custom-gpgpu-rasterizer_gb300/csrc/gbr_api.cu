@@ -282,6 +282,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     F.walk_base = r->d_walk; F.rank_next = &r->d_ctl->rank_next;
     F.ctl = r->d_ctl;
     F.scan_state = r->d_scan;
+    F.rec_tma = r->rec_tma;
     F.scan_spin_limit = r->scan_spin_limit;
     if (r->row1) {   // this renderer's share of a frame split by bin rows
         F.row0 = r->row0;
@@ -665,6 +666,12 @@ gbr_status gbr_set_raster_params(gbr_renderer* r, uint32_t phase, uint32_t ctas_
         GBR_CUDA(raster_configure(r->bw, r->bh, ctas_per_sm, &bps));
         r->raster_blocks_per_sm = std::max(bps, 1);
     }
+    return GBR_OK;
+}
+
+gbr_status gbr_set_raster_staging(gbr_renderer* r, uint32_t mode) {
+    if (!r || mode > GBR_STAGING_TMA) return fail(GBR_ERR_INVALID_ARG, "bad renderer or staging mode %u", mode);
+    r->rec_tma = mode == GBR_STAGING_TMA ? 1u : 0u;
     return GBR_OK;
 }
 

@@ -186,7 +186,8 @@ struct FrameDev {
     // (row1 = 0: every row; px_end = 0: every pixel)
     uint32_t row0, row1;
     uint32_t px_begin, px_end;
-    uint32_t rows_pad[3];
+    uint32_t rec_tma;          // raster: setup records staged by bulk asynchronous copies (1) or loads (0)
+    uint32_t rows_pad[2];
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 

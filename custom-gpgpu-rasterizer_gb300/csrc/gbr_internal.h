@@ -62,6 +62,7 @@ struct gbr_renderer {
     uint32_t raster_phase = 0;   // 0: library default
     uint32_t raster_ctas = 0;    // 0: library default
     uint32_t row0 = 0, row1 = 0;      // gbr_set_bin_rows: this renderer's bin rows (row1 0: all)
+    uint32_t rec_tma = 0;             // gbr_set_raster_staging: 1 = bulk asynchronous copies
     uint32_t scan_spin_limit = 0;     // gbr_set_scan_wait (0: the library's bound)
     uint32_t scan_silent_tile1 = 0;   // gbr_set_scan_wait: 1 + the silent tile (0: none)
     // the last finished frame's pair and visible-triangle counts: they size

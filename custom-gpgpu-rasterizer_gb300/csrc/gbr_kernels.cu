@@ -395,8 +395,56 @@ struct RasterShared {
     int next;
     uint32_t scene_next;         // batch: scene of the fetched work item
     uint32_t scene_loaded;       // batch: scene whose descriptor `frame` holds
+    __align__(8) unsigned long long rec_bar[2];   // mbarriers: a phase's setup records have landed (phases alternate)
     __align__(16) FrameDev frame;
 };
+
+// Setup records reach shared memory by bulk asynchronous copies (the TMA
+// engine's cp.async.bulk, one 48-byte copy per record), each completing
+// its bytes on one of the CTA's two mbarriers (phases alternate); readers
+// wait for that barrier's parity.  Warp 0 issues a phase's copies while the
+// phase before it rasterises, so they land in time.
+constexpr uint32_t kRecWaitLimit = 1u << 22;   // polls before a wait gives up (the frame is flagged)
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Warp 0 arms `bar` for `pn` records and copies the records of sorted
+// entries [p0, p0 + pn) into their ring slots (entry k -> slot k mod
+// kMaxPhase).
+__device__ __forceinline__ void issue_records(TriSetup* rec, const TriSetup* setup, const uint32_t* prim,
+                                              const uint16_t* order, uint32_t p0, uint32_t pn, uint32_t bar,
+                                              uint32_t lane);
+
+__device__ __forceinline__ void rec_copy(TriSetup* dst, const TriSetup* src, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 48, [%2];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void issue_records(TriSetup* rec, const TriSetup* setup, const uint32_t* prim,
+                                              const uint16_t* order, uint32_t p0, uint32_t pn, uint32_t bar,
+                                              uint32_t lane) {
+    if (lane == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(pn * 48u) : "memory");
+    __syncwarp();
+    for (uint32_t q = lane; q < pn; q += 32u) {
+        const uint32_t k = p0 + q;
+        rec_copy(&rec[k & (kMaxPhase - 1u)], setup + prim[order[k]], bar);
+    }
+}
+
+// Waits for phase `parity` of the mbarrier; false when the bound ran out.
+__device__ __forceinline__ bool rec_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kRecWaitLimit; ++it) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 
 // `key_bound` = hiz_key(t): a covered pixel whose stored key is already
 // below it cannot be won by this triangle, and skips the weights and depth.
@@ -524,7 +572,7 @@ __device__ __forceinline__ void fetch_item(uint4* dst, const uint4* items, uint3
 // (BATCH true): work items of all scenes of B; the scene of an item is
 // found from its global bin, and its frame descriptor is copied to shared
 // memory when it differs from the previous item's.
-template <int MIN_CTAS, bool BATCH>
+template <int MIN_CTAS, bool BATCH, bool TMA = false>
 __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameDev F, BatchDev B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     RasterShared& S = *reinterpret_cast<RasterShared*>(smem_raw);
@@ -544,7 +592,15 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
     // an item starts and its descriptor copied to shared memory
     // (asynchronously) while the item is staged
     uint32_t next_idx = 0;
+    constexpr bool tma = TMA;   // setup records staged by bulk copies (a variant for single frames)
+    const uint32_t rec_bar0 = smem_addr(&S.rec_bar[0]);
+    uint32_t rec_parity = 0;   // bit b: completions of record barrier b seen so far, mod 2
     if (tid == 0) {
+        if (TMA) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(rec_bar0) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(rec_bar0 + 8u) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
         next_idx = atomicAdd(&Q->item_next, 1u);
         fetch_item(&S.item_next, items, next_idx, num_items);
     }
@@ -640,8 +696,31 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
             // between phases.  A triangle whose key bound exceeds it cannot win
             // a pixel; once a whole bucket's lower bound does, the rest of the
             // batch is skipped.
-            for (uint32_t p0 = 0; p0 < total; p0 += phase) {
+            // TMA staging: phases of at most kMaxPhase / 2 triangles prefetch
+            // the next phase's records into the other half of the ring
+            const bool ahead = tma && phase <= kMaxPhase / 2u;
+            for (uint32_t p0 = 0, ph = 0; p0 < total; p0 += phase, ph ^= 1u) {
                 __syncthreads();   // the order, or the previous phase's records and tile
+                const uint32_t pn = min(phase, total - p0);
+                const uint32_t bar = rec_bar0 + 8u * ph, bar_next = rec_bar0 + 8u * (ph ^ 1u);
+                const bool next = ahead && p0 + phase < total;   // this phase prefetches the next one's records
+                if (tma) {
+                    if (warp == 0) {
+                        if (p0 == 0u || !ahead)   // this phase's records were not prefetched
+                            issue_records(S.rec, setup, S.prim, S.order, p0, pn, bar, lane);
+                        if (next)
+                            issue_records(S.rec, setup, S.prim, S.order, p0 + phase, min(phase, total - p0 - phase),
+                                          bar_next, lane);
+                    }
+                } else {
+                    // 16 bytes per thread (triangle k's record goes to slot k
+                    // mod kMaxPhase: phase <= kMaxPhase)
+                    for (uint32_t r = tid; r < 3u * pn; r += kRasterThreads) {
+                        const uint32_t q = r / 3u, k = p0 + q;
+                        const uint4* rp = reinterpret_cast<const uint4*>(setup) + 3u * S.prim[S.order[k]];
+                        reinterpret_cast<uint4*>(&S.rec[k & (kMaxPhase - 1u)])[r - 3u * q] = __ldg(rp + (r - 3u * q));
+                    }
+                }
                 if (b0 > 0 || p0 > 0) {
                     uint32_t m = 0;
                     for (int i = (int)tid; i < npx; i += kRasterThreads)
@@ -649,16 +728,15 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                     m = __reduce_max_sync(0xFFFFFFFFu, m);
                     if (lane == 0) S.warp_max[warp] = m;
                 }
-                // the phase's setup records, 16 bytes per thread
-                const uint32_t pn = min(phase, total - p0);
-                // (triangle k's record goes to slot k mod kMaxPhase: phase <= kMaxPhase)
-                for (uint32_t r = tid; r < 3u * pn; r += kRasterThreads) {
-                    const uint32_t q = r / 3u, k = p0 + q;
-                    const uint4* rp = reinterpret_cast<const uint4*>(setup) + 3u * S.prim[S.order[k]];
-                    reinterpret_cast<uint4*>(&S.rec[k & (kMaxPhase - 1u)])[r - 3u * q] = __ldg(rp + (r - 3u * q));
-                }
                 if (tid == 0) S.next = (int)p0;
                 __syncthreads();
+                // every thread sees this phase's records land before any phase
+                // decision; a phase that ends the batch early also waits for
+                // the records it prefetched, so no copy is ever left in flight
+                if (tma) {
+                    if (!rec_wait(bar, (rec_parity >> ph) & 1u) && tid == 0) atomicOr(&Q->error, 8u);
+                    rec_parity ^= 1u << ph;
+                }
                 uint32_t tile_max = 0xFFFFFFFFu;
                 if (b0 > 0 || p0 > 0) {
                     tile_max = 0;
@@ -667,7 +745,13 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                 }
                 // buckets [0, tile_max >> 23] can still hold a winner
                 const uint32_t limit = tile_max >= 0x80000000u ? total : S.bucket[tile_max >> 23];
-                if (p0 >= limit) break;   // uniform: every thread sees the same tile_max
+                if (p0 >= limit) {   // uniform: every thread sees the same tile_max
+                    if (next) {
+                        if (!rec_wait(bar_next, (rec_parity >> (ph ^ 1u)) & 1u) && tid == 0) atomicOr(&Q->error, 8u);
+                        rec_parity ^= 1u << (ph ^ 1u);
+                    }
+                    break;
+                }
                 const uint32_t p1 = min(limit, p0 + phase);
                 for (;;) {
                     int k = 0;
@@ -964,23 +1048,24 @@ cudaError_t launch_fill(const FrameDev& F, cudaStream_t s) {
     return launch_pdl(fill_kernel, dim3(blocks), dim3(256), 0, s, F);
 }
 
-template <bool BATCH>
+template <bool BATCH, bool TMA = false>
 static cudaError_t launch_raster_variant(const FrameDev& F, const BatchDev& B, uint32_t ctas, uint32_t grid, size_t smem,
                                          cudaStream_t s) {
     const dim3 g(grid), b(kRasterThreads);
     switch (ctas ? ctas : kDefaultRasterCtas) {
-        case 2: return launch_pdl(raster_kernel<2, BATCH>, g, b, smem, s, F, B);
-        case 3: return launch_pdl(raster_kernel<3, BATCH>, g, b, smem, s, F, B);
-        case 5: return launch_pdl(raster_kernel<5, BATCH>, g, b, smem, s, F, B);
-        case 6: return launch_pdl(raster_kernel<6, BATCH>, g, b, smem, s, F, B);
-        default: return launch_pdl(raster_kernel<4, BATCH>, g, b, smem, s, F, B);
+        case 2: return launch_pdl(raster_kernel<2, BATCH, TMA>, g, b, smem, s, F, B);
+        case 3: return launch_pdl(raster_kernel<3, BATCH, TMA>, g, b, smem, s, F, B);
+        case 5: return launch_pdl(raster_kernel<5, BATCH, TMA>, g, b, smem, s, F, B);
+        case 6: return launch_pdl(raster_kernel<6, BATCH, TMA>, g, b, smem, s, F, B);
+        default: return launch_pdl(raster_kernel<4, BATCH, TMA>, g, b, smem, s, F, B);
     }
 }
 
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
     BatchDev none;
     memset(&none, 0, sizeof none);
-    return launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
+    return F.rec_tma ? launch_raster_variant<false, true>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s)
+                     : launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
 }
 
 cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
@@ -1034,6 +1119,10 @@ template <int MIN_CTAS, bool BATCH>
 static cudaError_t configure_variant(size_t smem, int* blocks_per_sm) {
     cudaError_t e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (!BATCH) {   // the bulk-copy staging variant of a single frame
+        e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, raster_kernel<MIN_CTAS, BATCH>, kRasterThreads, smem);
 }
 

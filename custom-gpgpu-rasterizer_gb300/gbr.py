@@ -33,7 +33,7 @@ EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "g
             "gbr_mesh_bind_device", "gbr_mesh_set_world", "gbr_mesh_set_textures", "gbr_scene_clear",
             "gbr_texture_upload", "gbr_texture_remove", "gbr_set_lights", "gbr_set_binning", "gbr_set_predictor",
             "gbr_collect_bin_features", "gbr_predicted_capacities", "gbr_mlp_num_params", "gbr_mlp_predict", "gbr_mlp_loss_grad", "gbr_mlp_adam",
-            "gbr_set_raster_params", "gbr_set_scan_wait", "gbr_set_bin_rows", "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
+            "gbr_set_raster_params", "gbr_set_scan_wait", "gbr_set_bin_rows", "gbr_set_raster_staging", "gbr_set_timing", "gbr_render", "gbr_readback", "gbr_readback_ids", "gbr_device_buffers",
             "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
             "gbr_batch_set_view", "gbr_batch_set_config", "gbr_batch_get_config", "gbr_batch_autotune",
             "gbr_batch_set_timing", "gbr_batch_render", "gbr_batch_get_stats", "gbr_batch_scene_bins",
@@ -120,6 +120,7 @@ def lib():
             "gbr_set_timing": [vp, C.c_int],
             "gbr_set_scan_wait": [vp, u32, i32],
             "gbr_set_bin_rows": [vp, u32, u32],
+            "gbr_set_raster_staging": [vp, u32],
             "gbr_render": [vp, C.POINTER(Camera), u32, u32, u32, vp],
             "gbr_readback": [vp, vp, vp, vp],
             "gbr_readback_ids": [vp, vp, vp],
@@ -303,6 +304,10 @@ class Renderer:
 
     def set_raster_params(self, phase: int = 0, ctas_per_sm: int = 0):
         check(self._lib.gbr_set_raster_params(self.h, phase, ctas_per_sm))
+
+    def set_raster_staging(self, tma: bool):
+        """Setup records staged by bulk asynchronous copies (TMA) or loads."""
+        check(self._lib.gbr_set_raster_staging(self.h, 1 if tma else 0))
 
     def set_bin_rows(self, row0: int = 0, row1: int = 0):
         """This renderer's share of a frame split by bin rows: bin rows

@@ -221,6 +221,15 @@ gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
  * phase = triangles rasterised between hierarchical-z refreshes, 0..64 (0: 16),
  * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
 gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
+/* How the raster stages triangle-setup records into shared memory (no
+ * counterpart in the reference, whose RA_PerTileKernel reads them from global
+ * memory per pixel, CUDARenderer.cu:1039-1129): GBR_STAGING_LOADS (default),
+ * 16-byte loads by the CTA's threads; GBR_STAGING_TMA, one 48-byte bulk
+ * asynchronous copy (cp.async.bulk) per record completing on an mbarrier,
+ * the next phase's records copied while the current one rasterises.  Both
+ * give identical frames. */
+enum { GBR_STAGING_LOADS = 0, GBR_STAGING_TMA = 1 };
+gbr_status gbr_set_raster_staging(gbr_renderer *r, uint32_t mode);
 /* A frame split across GPUs by bin rows (no counterpart in the reference,
  * which renders on one GPU, main.cpp:397-399): the following frames of this
  * renderer bin and rasterise only bin rows [row0, row1) -- triangles are set

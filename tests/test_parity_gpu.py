@@ -339,3 +339,25 @@ def test_frame_split_by_bin_rows_composites_to_the_full_frame(gbr_lib, cuda_devi
         assert np.array_equal(got.view(np.uint32), full[key].view(np.uint32)), key
     # a triangle spanning a band boundary is binned by each band it touches
     assert pairs == full["stats"]["num_pairs"]
+
+
+@pytest.mark.parametrize("phase", [16, 64])
+@pytest.mark.parametrize("case", ["soup", "sphere", "strip"])
+def test_tma_record_staging_renders_identically(gbr_lib, cuda_device, case, phase):
+    """Setup records staged by bulk asynchronous copies on mbarriers
+    (GBR_STAGING_TMA): phase 16 prefetches the next phase's records, phase 64
+    copies each phase's own; bin lists, ids, depth and colour equal the
+    load-staged frame and the fixed-mode oracle."""
+    s = {"soup": lambda: scenes.soup_scene(60000, 640, 480, 16, seed=33), "sphere": scenes.sphere_scene,
+         "strip": scenes.strip_grid_scene}[case]()
+    out = []
+    for tma in (False, True):
+        r = gbr_lib.Renderer(s.width, s.height)
+        r.set_raster_params(phase=phase)
+        r.set_raster_staging(tma)
+        out.append(gpu_render(gbr_lib, s, renderer=r))
+        r.close()
+    for key in ("colour", "depth", "ids", "offsets", "bins"):
+        assert np.array_equal(out[0][key], out[1][key]), key
+    ofx = oracle.render(s, oracle.RASTER_FIXED)
+    assert_matches_fixed(out[1], ofx)
