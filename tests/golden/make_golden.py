@@ -11,7 +11,10 @@ reference produced:
     pixels for small cases, a band of rows for the 1080p case);
   * the per-bin triangle lists as sorted (bin, primitive id) pairs (small
     cases) or a sha256 of the sorted lists (1080p case), and the number of
-    visible triangles.
+    visible triangles;
+  * for the full-size cases, a 64-bit hash of every band of BAND_ROWS rows
+    of the whole framebuffer and of the whole zInterpolated frame
+    (band_hash), so tests can compare complete frames with the reference.
 
 usage: python tests/golden/make_golden.py OUT_DIR [case ...]
 """
@@ -56,7 +59,18 @@ CASES = {
     "soup1m_1080p": lambda: scenes.soup_scene(1_000_000, 1920, 1080, seed=0),
     "icosphere7_4k": lambda: scenes.icosphere_scene(),
 }
-FULL_SIZE = {"soup1m_1080p": (500, 532), "icosphere7_4k": (1064, 1096)}
+FULL_SIZE = {"soup1m_1080p": (500, 532), "icosphere7_4k": (1064, 1096)}   # the rows stored pixel by pixel
+BAND_ROWS = 8
+
+
+def band_hash(img):
+    """64-bit hashes (the first 8 bytes of sha256) of each band of
+    BAND_ROWS rows of a 4-byte-per-pixel frame, as uint64."""
+    a = np.ascontiguousarray(img).view(np.uint32)
+    out = []
+    for y0 in range(0, a.shape[0], BAND_ROWS):
+        out.append(int.from_bytes(hashlib.sha256(a[y0:y0 + BAND_ROWS].tobytes()).digest()[:8], "little"))
+    return np.array(out, np.uint64)
 
 
 def scene_hash(path):
@@ -90,6 +104,8 @@ def run_case(name, out_dir, harness):
         meta["rows"] = list(band)
         arrays["colour"] = res["colour"][band[0]:band[1]]
         arrays["z"] = res["z"][band[0]:band[1]]
+        arrays["colour_band_hash"] = band_hash(res["colour"])
+        arrays["z_band_hash"] = band_hash(res["z"])
     else:
         meta["rows"] = [0, scene.height]
         arrays["colour"] = res["colour"]

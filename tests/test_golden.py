@@ -88,3 +88,26 @@ def test_oracle_reproduces_reference(path):
         key_r, key_o = int(np.float32(zr) * np.float32(2 ** 31)), int(np.float32(zo) * np.float32(2 ** 31))
         assert key_r == key_o, f"non-tie mismatch at {(x, r0 + y)}: z ref {zr} oracle {zo}"
     assert len(bad) <= max(10, (r1 - r0) * meta["width"] // 1000), f"{len(bad)} tie pixels"
+
+
+FULL_FRAME = [p for p in FIXTURES if "z_band_hash" in np.load(p).files]
+
+
+@pytest.mark.skipif(not FULL_FRAME, reason="no full-frame band hashes")
+@pytest.mark.parametrize("path", FULL_FRAME, ids=[os.path.basename(p)[:-4] for p in FULL_FRAME])
+def test_oracle_reproduces_the_reference_full_frame(path):
+    """The full-size cases over their whole frames: the reference's
+    zInterpolated frame, hashed in bands of 8 rows, is reproduced bit for
+    bit by the oracle in reference mode on every band (so every pixel's
+    winning fragment agrees), and its framebuffer hash on nearly every band
+    (the rows the fixture stores are compared within 1 LSB above: a band
+    hash changes with a 1-LSB shading difference)."""
+    meta, arrays = load(path)
+    scene = scene_for(meta)
+    o = oracle.render(scene, oracle.RASTER_REFERENCE, want_bins=False)
+    z_same = make_golden.band_hash(o["depth"]) == arrays["z_band_hash"]
+    c_same = make_golden.band_hash(o["colour"]) == arrays["colour_band_hash"]
+    print(f"{meta['case']}: depth identical on {int(z_same.sum())}/{len(z_same)} bands, "
+          f"colour on {int(c_same.sum())}/{len(c_same)}")
+    assert z_same.all(), f"depth differs on bands {np.where(~z_same)[0][:10].tolist()}"
+    assert c_same.mean() >= 0.85
