@@ -785,10 +785,12 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
     return line
 
 
-def profile_frames(n: int, binning: str = "exact", workload: str = "soup", batch_scenes: int = BATCH_SCENES):
+def profile_frames(n: int, binning: str = "exact", workload: str = "soup", batch_scenes: int = BATCH_SCENES,
+                   staging: str = "loads"):
     """The benchmark's frame, device resident, n times on the default stream
-    (with the committed capacity model when binning is "predicted"); with
-    workload "icosphere" the lit 4K icosphere frame with 16x16 bins."""
+    (with the committed capacity model when binning is "predicted"; setup
+    records staged by TMA bulk copies with staging "tma"); with workload
+    "icosphere" the lit 4K icosphere frame with 16x16 bins."""
     import torch
     import gbr
 
@@ -836,6 +838,7 @@ def profile_frames(n: int, binning: str = "exact", workload: str = "soup", batch
     if binning == "predicted":
         import predictor
         predictor.install(r)
+    r.set_raster_staging(staging == "tma")
     for i in range(n):
         r.render_scene(scene)
         if i == 0:
@@ -864,6 +867,8 @@ def main():
                     help="scenes of the batch workload (its --profile-frames too)")
     ap.add_argument("--binning", choices=["exact", "predicted"], default="exact",
                     help="binning of the --profile-frames frames")
+    ap.add_argument("--staging", choices=["loads", "tma"], default="loads",
+                    help="raster setup-record staging of the --profile-frames frames")
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="render this many device-resident frames and exit (for a profiler)")
     args = ap.parse_args()
@@ -871,7 +876,7 @@ def main():
     if args.profile_frames:
         import build as gbr_build
         gbr_build.build()
-        profile_frames(args.profile_frames, args.binning, args.workload, args.batch_scenes)
+        profile_frames(args.profile_frames, args.binning, args.workload, args.batch_scenes, args.staging)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
