@@ -8,8 +8,8 @@ value   triangles/s of the whole job with the scene resident in HBM (CUDA
         256 MB write before every timed frame, outside the events).
 e2e     the same metric through the C ABI with host buffers: each step
         copies the vertices from pinned host memory, renders, and reads the
-        framebuffer back into pinned host memory; two renderers on two
-        streams, so step k+1's upload and frame overlap step k's readback
+        framebuffer back into pinned host memory; three renderers on three
+        streams, so each step's copies run under the other steps' frames
         (wall clock over all steps, an L2 flush queued with every step).
 roofline  the raster kernel (the dominant kernel): algorithmic bytes
         (4 B per bin entry read + 8 B per pixel written) / its CUDA-event
@@ -57,6 +57,7 @@ import numpy as np  # noqa: E402
 N_TRI = 1_000_000
 WIDTH, HEIGHT, BIN = 1920, 1080, 16
 CHUNK = 4096
+E2E_DEPTH = 3   # end-to-end leg: renderers (and streams) in flight
 METRIC = "triangles/s (1M-tri 1080p soup frame, exact two-pass binning)"
 UNIT = "triangles/s"
 WORKLOAD = "soup-1M-1080p"
@@ -414,35 +415,38 @@ def run_ours(args, rank, world, local):
 
     # end to end through the C ABI with host buffers -----------------------
     # Every step uploads its vertices from pinned host memory, renders, and
-    # reads its framebuffer back to pinned host memory.  Two renderers on two
-    # streams: step k+1's upload and frame are queued before step k's
-    # readback waits, as a streaming host would do.  The L2 flush is queued on
-    # every step's stream inside the timed region.
-    streams2 = [stream, torch.cuda.Stream(device=dev)]
+    # reads its framebuffer back to pinned host memory.  Three renderers on
+    # three streams (triple buffering, as a streaming host would do): steps
+    # k+1 and k+2 are queued before step k's readback waits, so the copies
+    # run under the other steps' frames.  The L2 flush is queued on every
+    # step's stream inside the timed region.
+    depth = E2E_DEPTH
+    streams_e = [stream] + [torch.cuda.Stream(device=dev) for _ in range(depth - 1)]
     rs = []
-    for _ in range(2):
+    for _ in range(depth):
         rr = gbr.Renderer(WIDTH, HEIGHT)
         rr.load_scene(scene, CHUNK)
         rs.append(rr)
     host_v = torch.from_numpy(mesh.vertices.view(np.uint8).copy()).pin_memory()
-    host_c = [torch.empty(WIDTH * HEIGHT, dtype=torch.int32).pin_memory() for _ in range(2)]
+    host_c = [torch.empty(WIDTH * HEIGHT, dtype=torch.int32).pin_memory() for _ in range(depth)]
     colour_np = [h.numpy().view(np.uint32) for h in host_c]
 
     def e2e_steps(n):
         for k in range(n):
-            i = k % 2
-            with torch.cuda.stream(streams2[i]):
+            i = k % depth
+            with torch.cuda.stream(streams_e[i]):
                 flush.zero_()
-            sp = streams2[i].cuda_stream
+            sp = streams_e[i].cuda_stream
             rs[i].update_vertices(0, host_v.data_ptr(), nv, sp)
             rs[i].render_scene(scene, sp)
-            if k > 0:
-                j = (k - 1) % 2
-                rs[j].readback(colour_np[j], stream=streams2[j].cuda_stream, want_depth=False)
-        j = (n - 1) % 2
-        rs[j].readback(colour_np[j], stream=streams2[j].cuda_stream, want_depth=False)
+            if k >= depth - 1:   # step k - depth + 1 is read back
+                j = (k - depth + 1) % depth
+                rs[j].readback(colour_np[j], stream=streams_e[j].cuda_stream, want_depth=False)
+        for k in range(max(n - depth + 1, 0), n):
+            j = k % depth
+            rs[j].readback(colour_np[j], stream=streams_e[j].cuda_stream, want_depth=False)
 
-    e2e_steps(max(args.warmup, 2))
+    e2e_steps(max(args.warmup, depth))
     torch.cuda.synchronize(dev)
     if dist:
         dist.barrier()
