@@ -629,13 +629,14 @@ def reference_cpu_batch(sl, workers: int, every: int = 8):
         return None
 
 
-# The batch autotuner's space: the workload's bin sizes and queue chunks,
-# and the raster variants (CTAs of 256 threads per SM).  Wider chunks are
-# tuned separately and reported beside it.
+# The batch autotuner's space: the workload's bin sizes, queue chunks and
+# threads per bin, and the raster variants (CTAs of 256 threads per SM).
+# Wider chunks are tuned separately and reported beside it.
 BATCH_BINS = (8, 16, 32)
 BATCH_CHUNKS = (32, 64, 128)
 BATCH_WIDE_CHUNKS = (512, 2048, 4096)
 BATCH_RASTER_CTAS = (5, 6)
+BATCH_RASTER_THREADS = (128, 256)
 
 
 def run_batch(args, rank, world, local, nested=False, dist=None):
@@ -678,7 +679,7 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
     with torch.cuda.stream(stream):
         # wider queue chunks than the workload names: tuned first, timed, reported as an extra
         wide_cfg = b.autotune(bin_sizes=BATCH_BINS, chunks=BATCH_WIDE_CHUNKS, raster_ctas=BATCH_RASTER_CTAS, frames=2,
-                              stream=sptr)
+                              stream=sptr, raster_threads=BATCH_RASTER_THREADS)
         b.set_timing(True)
         ms_w = []
         for _ in range(3):
@@ -687,7 +688,7 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
             ms_w.append(b.stats(sptr)["ms_frame"])
         wide = {"tuned": wide_cfg, "ms_frame": statistics.median(ms_w)}
         best = b.autotune(bin_sizes=BATCH_BINS, chunks=BATCH_CHUNKS, raster_ctas=BATCH_RASTER_CTAS, frames=2,
-                          stream=sptr)
+                          stream=sptr, raster_threads=BATCH_RASTER_THREADS)
     t_tune = time.perf_counter() - t0
     b.set_timing(True)
     with torch.cuda.stream(stream):
@@ -771,7 +772,8 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
                            "per_scene_triangles_per_s": n_tri / t_seq,
                            "batch_speedup_vs_per_scene": t_seq / t_batch,
                            "autotune_space": {"bins": BATCH_BINS, "queue_chunks": BATCH_CHUNKS,
-                                              "raster_ctas": BATCH_RASTER_CTAS},
+                                              "raster_ctas": BATCH_RASTER_CTAS,
+                                              "raster_threads": BATCH_RASTER_THREADS},
                            "wide_chunks": wide,
                            "l2": "256 MB write between timed frames"},
                 "e2e": {"value": n_tri / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,

@@ -52,7 +52,7 @@ struct gbr_batch {
     int device = 0;
     int num_sms = 0;
     std::vector<Member> members;
-    gbr_batch_config cfg{16u, 64u, 0u, 0u};
+    gbr_batch_config cfg{16u, 64u, 0u, 0u, 0u};
     bool timing = false;
 
     // layout
@@ -105,6 +105,9 @@ struct gbr_batch {
 namespace {
 
 uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1u) / b); }
+
+// raster CTA width of a configuration (0: 256)
+uint32_t raster_threads(const gbr_batch_config& c) { return c.raster_threads == 128u ? 128u : 256u; }
 
 void drop_graph(gbr_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -247,7 +250,7 @@ gbr_status ensure_layout(gbr_batch* b) {
     b->last_table.clear();
 
     int bps = 0;
-    GBR_CUDA(raster_configure_batch(bs, bs, b->cfg.raster_ctas, &bps));
+    GBR_CUDA(raster_configure_batch(bs, bs, b->cfg.raster_ctas, raster_threads(b->cfg), &bps));
     b->raster_bps = std::max(bps, 1);
     b->layout_valid = true;
     return GBR_OK;
@@ -321,6 +324,7 @@ gbr_status capture_graph(gbr_batch* b) {
     L.px_blocks = b->px_blocks;
     L.raster_grid = (uint32_t)(b->num_sms * b->raster_bps);
     L.raster_ctas = b->cfg.raster_ctas;
+    L.raster_threads = raster_threads(b->cfg);
     L.bin_w = L.bin_h = b->cfg.bin_size;
     const BatchDev B = batch_dev(b);
     memset(&L.scan, 0, sizeof L.scan);
@@ -434,9 +438,11 @@ gbr_status check_state(uint32_t cull, uint32_t sample, uint32_t vis) {
 
 gbr_status check_config(const gbr_batch_config& c) {
     if (c.bin_size == 0 || c.bin_size > (uint32_t)kMaxBinDim || c.queue_chunk == 0 || c.raster_phase > kMaxPhase ||
-        (c.raster_ctas != 0 && (c.raster_ctas < 2 || c.raster_ctas > 6)))
-        return fail(GBR_ERR_INVALID_ARG, "batch config: bin %u (1..%d), chunk %u (>= 1), ctas %u (0, 2..6), phase %u",
-                    c.bin_size, kMaxBinDim, c.queue_chunk, c.raster_ctas, c.raster_phase);
+        (c.raster_ctas != 0 && (c.raster_ctas < 2 || c.raster_ctas > 6)) ||
+        (c.raster_threads != 0 && c.raster_threads != 128 && c.raster_threads != 256))
+        return fail(GBR_ERR_INVALID_ARG,
+                    "batch config: bin %u (1..%d), chunk %u (>= 1), ctas %u (0, 2..6), phase %u, threads %u (0, 128, 256)",
+                    c.bin_size, kMaxBinDim, c.queue_chunk, c.raster_ctas, c.raster_phase, c.raster_threads);
     return GBR_OK;
 }
 
@@ -541,7 +547,8 @@ gbr_status gbr_batch_render(gbr_batch* b, void* stream) {
 
 gbr_status gbr_batch_autotune(gbr_batch* b, const uint32_t* bin_sizes, uint32_t num_bin_sizes, const uint32_t* chunks,
                               uint32_t num_chunks, const uint32_t* raster_ctas, uint32_t num_raster_ctas,
-                              uint32_t frames, void* stream, gbr_batch_config* best) {
+                              const uint32_t* raster_threads, uint32_t num_raster_threads, uint32_t frames, void* stream,
+                              gbr_batch_config* best) {
     if (!b) return fail(GBR_ERR_INVALID_ARG, "batch is null");
     if (b->members.empty()) return fail(GBR_ERR_INVALID_ARG, "the batch has no scenes");
     cudaStream_t s = (cudaStream_t)stream;
@@ -553,6 +560,9 @@ gbr_status gbr_batch_autotune(gbr_batch* b, const uint32_t* bin_sizes, uint32_t 
     std::vector<uint32_t> rl = raster_ctas && num_raster_ctas
                                    ? std::vector<uint32_t>(raster_ctas, raster_ctas + num_raster_ctas)
                                    : std::vector<uint32_t>{base.raster_ctas};
+    std::vector<uint32_t> tl = raster_threads && num_raster_threads
+                                   ? std::vector<uint32_t>(raster_threads, raster_threads + num_raster_threads)
+                                   : std::vector<uint32_t>{base.raster_threads};
     if (frames == 0) frames = 1;
     const bool timing = b->timing;
     b->timing = true;
@@ -561,11 +571,13 @@ gbr_status gbr_batch_autotune(gbr_batch* b, const uint32_t* bin_sizes, uint32_t 
     gbr_status st = GBR_OK;
     for (uint32_t bs : bl)
         for (uint32_t ch : cl)
-            for (uint32_t rc : rl) {
+            for (uint32_t rc : rl)
+            for (uint32_t rt : tl) {
                 gbr_batch_config c = base;
                 c.bin_size = bs;
                 c.queue_chunk = ch;
                 c.raster_ctas = rc;
+                c.raster_threads = rt;
                 st = gbr_batch_set_config(b, &c);
                 if (st != GBR_OK) goto done;
                 // warm-up frame: sizes the storage (overflow re-render) and captures the graph

@@ -382,14 +382,26 @@ cudaError_t launch_list_touch(const FrameDev& F, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // Raster + ROP + shade
 // ---------------------------------------------------------------------------
-struct RasterShared {
+// A raster CTA of THREADS threads stages 8 entries per thread at once and
+// sorts them into THREADS depth buckets (one per thread): the top
+// log2(THREADS) bits of the 31-bit depth key.
+template <int THREADS>
+struct RasterGeom {
+    static_assert(THREADS == 128 || THREADS == 256, "raster CTAs of 128 or 256 threads");
+    static constexpr uint32_t kEntries = 8u * THREADS;             // entries depth-sorted at once
+    static constexpr uint32_t kKeyShift = THREADS == 256 ? 23u : 24u;   // depth key -> bucket
+};
+static_assert(RasterGeom<kRasterThreads>::kEntries == (uint32_t)kBatch, "the 256-thread raster sorts kBatch entries");
+
+template <int THREADS>
+struct RasterSharedT {
     TriSetup rec[kMaxPhase];     // setup records of the running phase
-    uint32_t prim[kBatch];       // staged bin entries (rasterisable triangles)
-    uint32_t key[kBatch];        // their depth-key lower bounds
-    uint16_t order[kBatch];      // staged triangles, front to back by depth bucket
-    uint32_t bucket[kDepthBuckets];   // counts -> starts -> (after the scatter) ends
-    uint32_t warp_count[kRasterThreads / 32];
-    uint32_t warp_max[kRasterThreads / 32];
+    uint32_t prim[RasterGeom<THREADS>::kEntries];   // staged bin entries (rasterisable triangles)
+    uint32_t key[RasterGeom<THREADS>::kEntries];    // their depth-key lower bounds
+    uint16_t order[RasterGeom<THREADS>::kEntries];  // staged triangles, front to back by depth bucket
+    uint32_t bucket[THREADS];    // counts -> starts -> (after the scatter) ends
+    uint32_t warp_count[THREADS / 32];
+    uint32_t warp_max[THREADS / 32];
     uint32_t item[4];
     __align__(16) uint4 item_next;   // the next work item, copied ahead by thread 0
     int next;
@@ -398,6 +410,7 @@ struct RasterShared {
     __align__(8) unsigned long long rec_bar[2];   // mbarriers: a phase's setup records have landed (phases alternate)
     __align__(16) FrameDev frame;
 };
+using RasterShared = RasterSharedT<kRasterThreads>;
 
 // Setup records reach shared memory by bulk asynchronous copies (the TMA
 // engine's cp.async.bulk, one 48-byte copy per record), each completing
@@ -572,11 +585,15 @@ __device__ __forceinline__ void fetch_item(uint4* dst, const uint4* items, uint3
 // (BATCH true): work items of all scenes of B; the scene of an item is
 // found from its global bin, and its frame descriptor is copied to shared
 // memory when it differs from the previous item's.
-template <int MIN_CTAS, bool BATCH, bool TMA = false>
-__global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameDev F, BatchDev B) {
+// MIN_CTAS counts CTAs of 256 threads: a 128-thread variant keeps twice as
+// many resident (the same registers per thread).
+template <int MIN_CTAS, bool BATCH, bool TMA = false, int THREADS = kRasterThreads>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS * (kRasterThreads / THREADS)) raster_kernel(FrameDev F, BatchDev B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    RasterShared& S = *reinterpret_cast<RasterShared*>(smem_raw);
-    unsigned long long* tile = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(RasterShared));
+    using Shared = RasterSharedT<THREADS>;
+    constexpr uint32_t kEntries = RasterGeom<THREADS>::kEntries, kKeyShift = RasterGeom<THREADS>::kKeyShift;
+    Shared& S = *reinterpret_cast<Shared*>(smem_raw);
+    unsigned long long* tile = reinterpret_cast<unsigned long long*>(smem_raw + sizeof(Shared));
     pdl_wait();
     Ctl* const Q = BATCH ? B.ctl : F.ctl;
     const uint4* const items = BATCH ? B.items : F.items;
@@ -586,7 +603,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
     const uint32_t phase_req = BATCH ? B.phase : F.phase;
     const uint32_t phase = phase_req == 0u ? kPhase : min(phase_req, kMaxPhase);
     const uint32_t stage_req = BATCH ? B.stage : F.stage;
-    const uint32_t pass = stage_req == 0u ? kBatch : min(stage_req, kBatch);   // entries per raster pass
+    const uint32_t pass = stage_req == 0u ? kEntries : min(stage_req, kEntries);   // entries per raster pass
     if (BATCH && tid == 0) S.scene_loaded = 0xFFFFFFFFu;
     // thread 0 runs one item ahead: the next item's queue slot is taken when
     // an item starts and its descriptor copied to shared memory
@@ -624,7 +641,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
             if (sc != S.scene_loaded) {   // uniform across the CTA
                 const uint4* src = reinterpret_cast<const uint4*>(B.scenes + sc);
                 uint4* dst = reinterpret_cast<uint4*>(&S.frame);
-                for (uint32_t i = tid; i < sizeof(FrameDev) / 16u; i += kRasterThreads) dst[i] = __ldg(src + i);
+                for (uint32_t i = tid; i < sizeof(FrameDev) / 16u; i += THREADS) dst[i] = __ldg(src + i);
                 __syncthreads();
                 if (tid == 0) S.scene_loaded = sc;
             }
@@ -638,28 +655,27 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
         const TriSetup* const setup = G.setup;
         unsigned long long* const gvis = G.gvis;
         const uint32_t width = G.width;
-        for (int i = (int)tid; i < npx; i += kRasterThreads) tile[i] = kEmptyVis;
+        for (int i = (int)tid; i < npx; i += THREADS) tile[i] = kEmptyVis;
         if (tid == 0) fetch_item(&S.item_next, items, next_idx, num_items);
         const uint32_t* const keys = G.keys;
         for (uint32_t b0 = 0; b0 < count && npx > 0; b0 += pass) {
             // stage the entries with their depth-key bounds (no setup record
             // is read before a triangle's phase comes) and count the
             // rasterisable ones per depth bucket
-            constexpr uint32_t kPer = kBatch / kRasterThreads;
-            static_assert(kDepthBuckets == kRasterThreads, "one bucket per thread");
+            constexpr uint32_t kPer = kEntries / THREADS;
             const uint32_t n = min(pass, count - b0);
             __syncthreads();   // the previous batch is done with the shared arrays
             S.bucket[tid] = 0u;
             __syncthreads();
 #pragma unroll 4
             for (uint32_t j = 0; j < kPer; ++j) {
-                const uint32_t idx = j * kRasterThreads + tid;
+                const uint32_t idx = j * THREADS + tid;
                 const uint32_t e = idx < n ? __ldg(list + start + b0 + idx) : kNoRasterBit;
                 const bool keep = !(e & kNoRasterBit);
                 const uint32_t k = keep ? __ldg(keys + e) : 0u;
                 S.prim[idx] = e;
                 S.key[idx] = k;
-                if (keep) atomicAdd(&S.bucket[k >> 23], 1u);
+                if (keep) atomicAdd(&S.bucket[k >> kKeyShift], 1u);
             }
             __syncthreads();
             // bucket starts: exclusive scan of the 256 counts; their sum is the
@@ -677,7 +693,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                 __syncthreads();
                 uint32_t before = 0;
 #pragma unroll
-                for (uint32_t w = 0; w < kRasterThreads / 32; ++w) {
+                for (uint32_t w = 0; w < THREADS / 32; ++w) {
                     const uint32_t wc = S.warp_count[w];
                     before += w < warp ? wc : 0u;
                     total += wc;
@@ -687,9 +703,9 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
             __syncthreads();
 #pragma unroll
             for (uint32_t j = 0; j < kPer; ++j) {
-                const uint32_t idx = j * kRasterThreads + tid;
+                const uint32_t idx = j * THREADS + tid;
                 if (idx < n && !(S.prim[idx] & kNoRasterBit))
-                    S.order[atomicAdd(&S.bucket[S.key[idx] >> 23], 1u)] = (uint16_t)idx;
+                    S.order[atomicAdd(&S.bucket[S.key[idx] >> kKeyShift], 1u)] = (uint16_t)idx;
             }
             // now S.bucket[b] = end of bucket b
             // phases of `phase` triangles; the tile's max depth key is refreshed
@@ -715,7 +731,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                 } else {
                     // 16 bytes per thread (triangle k's record goes to slot k
                     // mod kMaxPhase: phase <= kMaxPhase)
-                    for (uint32_t r = tid; r < 3u * pn; r += kRasterThreads) {
+                    for (uint32_t r = tid; r < 3u * pn; r += THREADS) {
                         const uint32_t q = r / 3u, k = p0 + q;
                         const uint4* rp = reinterpret_cast<const uint4*>(setup) + 3u * S.prim[S.order[k]];
                         reinterpret_cast<uint4*>(&S.rec[k & (kMaxPhase - 1u)])[r - 3u * q] = __ldg(rp + (r - 3u * q));
@@ -723,7 +739,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                 }
                 if (b0 > 0 || p0 > 0) {
                     uint32_t m = 0;
-                    for (int i = (int)tid; i < npx; i += kRasterThreads)
+                    for (int i = (int)tid; i < npx; i += THREADS)
                         m = max(m, (uint32_t)(tile[i] >> 32));
                     m = __reduce_max_sync(0xFFFFFFFFu, m);
                     if (lane == 0) S.warp_max[warp] = m;
@@ -741,10 +757,10 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
                 if (b0 > 0 || p0 > 0) {
                     tile_max = 0;
 #pragma unroll
-                    for (uint32_t w = 0; w < kRasterThreads / 32; ++w) tile_max = max(tile_max, S.warp_max[w]);
+                    for (uint32_t w = 0; w < THREADS / 32; ++w) tile_max = max(tile_max, S.warp_max[w]);
                 }
-                // buckets [0, tile_max >> 23] can still hold a winner
-                const uint32_t limit = tile_max >= 0x80000000u ? total : S.bucket[tile_max >> 23];
+                // buckets [0, tile_max >> kKeyShift] can still hold a winner
+                const uint32_t limit = tile_max >= 0x80000000u ? total : S.bucket[tile_max >> kKeyShift];
                 if (p0 >= limit) {   // uniform: every thread sees the same tile_max
                     if (next) {
                         if (!rec_wait(bar_next, (rec_parity >> (ph ^ 1u)) & 1u) && tid == 0) atomicOr(&Q->error, 8u);
@@ -770,7 +786,7 @@ __global__ void __launch_bounds__(kRasterThreads, MIN_CTAS) raster_kernel(FrameD
         // publish the tile: one chunk owns its pixels (plain stores); the
         // chunks of a longer bin merge with 64-bit atomicMin
         if (npx > 0 && count > 0) {
-            for (int i = (int)tid; i < npx; i += kRasterThreads) {
+            for (int i = (int)tid; i < npx; i += THREADS) {
                 const unsigned long long v = tile[i];
                 unsigned long long* g = &gvis[(size_t)(ty0 + i / tw) * width + (size_t)(tx0 + i % tw)];
                 if (nchunks == 1u) *g = v;
@@ -982,8 +998,9 @@ __global__ void __launch_bounds__(256) batch_shade_kernel(BatchDev B, uint32_t c
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
-size_t raster_smem_bytes(uint32_t bw, uint32_t bh) {
-    return sizeof(RasterShared) + (size_t)bw * bh * sizeof(unsigned long long);
+size_t raster_smem_bytes(uint32_t bw, uint32_t bh, uint32_t threads) {
+    const size_t shared = threads == 128u ? sizeof(RasterSharedT<128>) : sizeof(RasterSharedT<256>);
+    return shared + (size_t)bw * bh * sizeof(unsigned long long);
 }
 
 // Blocks of 256 threads for a triangle pass: one per 256 triangles, at most
@@ -1048,16 +1065,16 @@ cudaError_t launch_fill(const FrameDev& F, cudaStream_t s) {
     return launch_pdl(fill_kernel, dim3(blocks), dim3(256), 0, s, F);
 }
 
-template <bool BATCH, bool TMA = false>
+template <bool BATCH, bool TMA = false, int THREADS = kRasterThreads>
 static cudaError_t launch_raster_variant(const FrameDev& F, const BatchDev& B, uint32_t ctas, uint32_t grid, size_t smem,
                                          cudaStream_t s) {
-    const dim3 g(grid), b(kRasterThreads);
+    const dim3 g(grid), b(THREADS);
     switch (ctas ? ctas : kDefaultRasterCtas) {
-        case 2: return launch_pdl(raster_kernel<2, BATCH, TMA>, g, b, smem, s, F, B);
-        case 3: return launch_pdl(raster_kernel<3, BATCH, TMA>, g, b, smem, s, F, B);
-        case 5: return launch_pdl(raster_kernel<5, BATCH, TMA>, g, b, smem, s, F, B);
-        case 6: return launch_pdl(raster_kernel<6, BATCH, TMA>, g, b, smem, s, F, B);
-        default: return launch_pdl(raster_kernel<4, BATCH, TMA>, g, b, smem, s, F, B);
+        case 2: return launch_pdl(raster_kernel<2, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
+        case 3: return launch_pdl(raster_kernel<3, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
+        case 5: return launch_pdl(raster_kernel<5, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
+        case 6: return launch_pdl(raster_kernel<6, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
+        default: return launch_pdl(raster_kernel<4, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
     }
 }
 
@@ -1101,7 +1118,9 @@ cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s
     if (L.tri_blocks) batch_fill_kernel<<<L.tri_blocks, 256, 0, s>>>(B);
     FrameDev none;
     memset(&none, 0, sizeof none);
-    e = launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, raster_smem_bytes(L.bin_w, L.bin_h), s);
+    const size_t smem = raster_smem_bytes(L.bin_w, L.bin_h, L.raster_threads);
+    e = L.raster_threads == 128u ? launch_raster_variant<true, false, 128>(none, B, L.raster_ctas, L.raster_grid, smem, s)
+                                 : launch_raster_variant<true>(none, B, L.raster_ctas, L.raster_grid, smem, s);
     if (e != cudaSuccess) return e;
     if (L.px_blocks) {
         if (B.all_flat) batch_shade_kernel<true><<<px_grid, 256, 0, s>>>(B, L.px_blocks, px_per);
@@ -1115,26 +1134,28 @@ cudaError_t launch_clear(const FrameDev& F, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <int MIN_CTAS, bool BATCH>
+template <int MIN_CTAS, bool BATCH, int THREADS>
 static cudaError_t configure_variant(size_t smem, int* blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, BATCH, false, THREADS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (!BATCH) {   // the bulk-copy staging variant of a single frame
         e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, raster_kernel<MIN_CTAS, BATCH>, kRasterThreads, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, raster_kernel<MIN_CTAS, BATCH, false, THREADS>,
+                                                         THREADS, smem);
 }
 
-template <bool BATCH>
+template <bool BATCH, int THREADS = kRasterThreads>
 static cudaError_t configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm) {
-    const size_t smem = raster_smem_bytes(bw, bh);
+    const size_t smem = raster_smem_bytes(bw, bh, THREADS);
     switch (ctas ? ctas : kDefaultRasterCtas) {
-        case 2: return configure_variant<2, BATCH>(smem, blocks_per_sm);
-        case 3: return configure_variant<3, BATCH>(smem, blocks_per_sm);
-        case 5: return configure_variant<5, BATCH>(smem, blocks_per_sm);
-        case 6: return configure_variant<6, BATCH>(smem, blocks_per_sm);
-        default: return configure_variant<4, BATCH>(smem, blocks_per_sm);
+        case 2: return configure_variant<2, BATCH, THREADS>(smem, blocks_per_sm);
+        case 3: return configure_variant<3, BATCH, THREADS>(smem, blocks_per_sm);
+        case 5: return configure_variant<5, BATCH, THREADS>(smem, blocks_per_sm);
+        case 6: return configure_variant<6, BATCH, THREADS>(smem, blocks_per_sm);
+        default: return configure_variant<4, BATCH, THREADS>(smem, blocks_per_sm);
     }
 }
 
@@ -1142,8 +1163,8 @@ cudaError_t raster_configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* block
     return configure<false>(bw, bh, ctas, blocks_per_sm);
 }
 
-cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm) {
-    return configure<true>(bw, bh, ctas, blocks_per_sm);
+cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, uint32_t threads, int* blocks_per_sm) {
+    return threads == 128u ? configure<true, 128>(bw, bh, ctas, blocks_per_sm) : configure<true>(bw, bh, ctas, blocks_per_sm);
 }
 
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm) {

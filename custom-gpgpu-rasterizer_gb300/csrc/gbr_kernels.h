@@ -30,7 +30,8 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-size_t raster_smem_bytes(uint32_t bw, uint32_t bh);
+// threads: raster CTA width (128 or 256)
+size_t raster_smem_bytes(uint32_t bw, uint32_t bh, uint32_t threads = 256);
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, int* blocks_per_sm);
 // ctas: the raster_kernel variant compiled for 2..6 CTAs per SM (0: default)
 cudaError_t raster_configure(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
@@ -54,12 +55,13 @@ struct BatchLaunch {
     uint32_t px_blocks;     // shade blocks of all scenes
     uint32_t raster_grid;   // persistent raster CTAs
     uint32_t raster_ctas;   // raster variant (CTAs per SM it is compiled for; 0: default)
+    uint32_t raster_threads;   // raster CTA width: 128 or 256
     uint32_t bin_w, bin_h;  // the largest bin of the batch (shared-memory tile)
     ScanDev scan;           // the scan over the bins of every scene
 };
 // reset, setup + count, bin scan (three launches), fill, raster, shade
 cudaError_t launch_batch(const BatchDev& B, const BatchLaunch& L, cudaStream_t s);
-cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, int* blocks_per_sm);
+cudaError_t raster_configure_batch(uint32_t bw, uint32_t bh, uint32_t ctas, uint32_t threads, int* blocks_per_sm);
 
 // Message returned by gbr_last_error_string() on the calling thread.
 void set_last_error(const char* msg);

@@ -71,7 +71,7 @@ class ObjMesh(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("bin_size", C.c_uint32), ("queue_chunk", C.c_uint32), ("raster_ctas", C.c_uint32),
-                ("raster_phase", C.c_uint32)]
+                ("raster_phase", C.c_uint32), ("raster_threads", C.c_uint32)]
 
 
 class BatchStats(C.Structure):
@@ -135,7 +135,7 @@ def lib():
             "gbr_batch_set_view": [vp, u32, C.POINTER(Camera), u32, u32, u32],
             "gbr_batch_set_config": [vp, C.POINTER(BatchConfig)],
             "gbr_batch_get_config": [vp, C.POINTER(BatchConfig)],
-            "gbr_batch_autotune": [vp, vp, u32, vp, u32, vp, u32, u32, vp, C.POINTER(BatchConfig)],
+            "gbr_batch_autotune": [vp, vp, u32, vp, u32, vp, u32, vp, u32, u32, vp, C.POINTER(BatchConfig)],
             "gbr_batch_set_timing": [vp, C.c_int],
             "gbr_batch_render": [vp, vp],
             "gbr_batch_get_stats": [vp, C.POINTER(BatchStats), vp],
@@ -444,8 +444,9 @@ class Batch:
         cam = camera if isinstance(camera, Camera) else make_camera(camera)
         check(self._lib.gbr_batch_set_view(self.h, index, C.byref(cam), cull, sample, vis))
 
-    def set_config(self, bin_size: int = 16, queue_chunk: int = 64, raster_ctas: int = 0, raster_phase: int = 0):
-        cfg = BatchConfig(bin_size, queue_chunk, raster_ctas, raster_phase)
+    def set_config(self, bin_size: int = 16, queue_chunk: int = 64, raster_ctas: int = 0, raster_phase: int = 0,
+                   raster_threads: int = 0):
+        cfg = BatchConfig(bin_size, queue_chunk, raster_ctas, raster_phase, raster_threads)
         check(self._lib.gbr_batch_set_config(self.h, C.byref(cfg)))
 
     def config(self) -> dict:
@@ -454,12 +455,14 @@ class Batch:
         return {k: getattr(cfg, k) for k, _ in BatchConfig._fields_}
 
     def autotune(self, bin_sizes=(8, 16, 32), chunks=(128, 512, 2048), raster_ctas=None, frames: int = 2,
-                 stream: int = 0) -> dict:
+                 stream: int = 0, raster_threads=None) -> dict:
         b, nb = _u32_list(bin_sizes)
         c, nc = _u32_list(chunks)
         r, nr = _u32_list(raster_ctas)
+        t, nt = _u32_list(raster_threads)
         best = BatchConfig()
-        check(self._lib.gbr_batch_autotune(self.h, b, nb, c, nc, r, nr, frames, _stream(stream), C.byref(best)))
+        check(self._lib.gbr_batch_autotune(self.h, b, nb, c, nc, r, nr, t, nt, frames, _stream(stream),
+                                           C.byref(best)))
         return {k: getattr(best, k) for k, _ in BatchConfig._fields_}
 
     def set_timing(self, on: bool):

@@ -294,8 +294,11 @@ typedef struct {
     uint32_t bin_size;     /* bins of bin_size x bin_size pixels, 1..64 */
     uint32_t queue_chunk;  /* entries depth-sorted and rasterised per pass over a tile, >= 1 (at most 2048
                               used); work items hold 2048 entries */
-    uint32_t raster_ctas;  /* raster variant: CTAs per SM, 2..6 (0: 6) */
+    uint32_t raster_ctas;  /* raster variant: CTAs per SM, 2..6 (0: 6), counted in CTAs of 256 threads */
     uint32_t raster_phase; /* triangles between hierarchical-z refreshes, 0..64 (0: 16) */
+    uint32_t raster_threads; /* threads per bin: raster CTAs of 128 or 256 threads (0: 256); a 128-thread CTA
+                                depth-sorts 1024 entries at a time into 128 buckets, and twice raster_ctas
+                                of them are resident per SM */
 } gbr_batch_config;
 typedef struct {
     uint32_t num_scenes;
@@ -318,12 +321,13 @@ gbr_status gbr_batch_set_view(gbr_batch *b, uint32_t index, const gbr_camera *ca
 gbr_status gbr_batch_set_config(gbr_batch *b, const gbr_batch_config *cfg);
 gbr_status gbr_batch_get_config(const gbr_batch *b, gbr_batch_config *cfg);
 /* Times `frames` batch frames (after one warm-up frame) for every
- * combination of the candidate bin sizes, queue chunks and raster variants
- * (a NULL list keeps the current value) and keeps the fastest; *best gets
- * it.  Synchronises `stream`. */
+ * combination of the candidate bin sizes, queue chunks, raster variants
+ * (CTAs per SM) and threads per bin (a NULL list keeps the current value)
+ * and keeps the fastest; *best gets it.  Synchronises `stream`. */
 gbr_status gbr_batch_autotune(gbr_batch *b, const uint32_t *bin_sizes, uint32_t num_bin_sizes, const uint32_t *chunks,
                               uint32_t num_chunks, const uint32_t *raster_ctas, uint32_t num_raster_ctas,
-                              uint32_t frames, void *stream, gbr_batch_config *best);
+                              const uint32_t *raster_threads, uint32_t num_raster_threads, uint32_t frames,
+                              void *stream, gbr_batch_config *best);
 gbr_status gbr_batch_set_timing(gbr_batch *b, int enabled);
 /* One batch frame on `stream`, without host synchronisation. */
 gbr_status gbr_batch_render(gbr_batch *b, void *stream);

@@ -77,11 +77,16 @@ def assert_batch_equals_single(gbr, b, scene_list, bin_size, chunk):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bin_size,chunk", [(16, 64), (8, 32), (32, 128), (16, 4096)])
-def test_batch_equals_single_frames(gbr_lib, cuda_device, bin_size, chunk):
+@pytest.mark.parametrize("bin_size,chunk,threads", [(16, 64, 256), (8, 32, 256), (32, 128, 256), (16, 4096, 256),
+                                                    (16, 64, 128), (8, 32, 128), (32, 128, 128), (16, 4096, 128)])
+def test_batch_equals_single_frames(gbr_lib, cuda_device, bin_size, chunk, threads):
+    """Every scene of a batch frame equals its single frame, for 256- and
+    128-thread raster CTAs (a 128-thread CTA depth-sorts 1024 entries at a
+    time into 128 buckets: a 4096-entry queue chunk takes four passes)."""
     sl = mixed_scenes()
     b, rs = build_batch(gbr_lib, sl)
-    b.set_config(bin_size, chunk)
+    b.set_config(bin_size, chunk, raster_threads=threads)
+    assert b.config()["raster_threads"] == threads
     b.render()
     st = b.stats()
     assert st["num_scenes"] == len(sl) and st["graph_captures"] >= 1
@@ -175,9 +180,10 @@ def test_batch_autotune_keeps_output(gbr_lib, cuda_device):
     b.set_config(16, 64)
     b.render()
     before = [b.readback(i) for i in range(len(sl))]
-    best = b.autotune(bin_sizes=(8, 16, 32), chunks=(32, 64, 128), raster_ctas=(4, 5), frames=1)
+    best = b.autotune(bin_sizes=(8, 16, 32), chunks=(32, 64, 128), raster_ctas=(4, 5), frames=1,
+                      raster_threads=(128, 256))
     assert best["bin_size"] in (8, 16, 32) and best["queue_chunk"] in (32, 64, 128)
-    assert best["raster_ctas"] in (4, 5)
+    assert best["raster_ctas"] in (4, 5) and best["raster_threads"] in (128, 256)
     assert b.config() == best
     b.render()
     for i in range(len(sl)):
