@@ -733,25 +733,52 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
             seq.append(ev0.elapsed_time(ev1))
     t_seq = statistics.mean(seq) / 1e3
 
-    # end to end: vertices from pinned host memory, batch frame, colour back
+    # end to end: vertices from pinned host memory, batch frame, colours
+    # back.  Two batches of the same scenes (two renderer sets) on two
+    # streams: batch step k+1's uploads and frame are queued before step k's
+    # readbacks wait, as a streaming host would do; wall clock over all steps.
     hosts = [torch.from_numpy(s.meshes[0].vertices.view(np.uint8).copy()).pin_memory() for s in sl]
-    outs = [torch.empty(s.width * s.height, dtype=torch.int32).pin_memory() for s in sl]
+    outs = [[torch.empty(s.width * s.height, dtype=torch.int32).pin_memory() for s in sl] for _ in range(2)]
     h2d = sum(h.numel() for h in hosts)
-    d2h = sum(o.numel() * 4 for o in outs)
-    e2e = []
-    with torch.cuda.stream(stream):
-        for step in range(args.warmup + args.steps):
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            for r, h, s in zip(rs, hosts, sl):
-                r.update_vertices(0, h.data_ptr(), len(s.meshes[0].vertices), sptr)
-            b.render(sptr)
-            for i, o in enumerate(outs):
-                gbr.check(b._lib.gbr_batch_readback(b.h, i, gbr.C.c_void_p(o.data_ptr()), None, None,
-                                                    gbr.C.c_void_p(sptr)))
-            if step >= args.warmup:
-                e2e.append(time.perf_counter() - t0)
-    t_e2e = statistics.mean(e2e)
+    d2h = sum(o.numel() * 4 for o in outs[0])
+    rs2 = []
+    for s in sl:
+        r = gbr.Renderer(s.width, s.height)
+        r.load_scene(s, CHUNK)
+        rs2.append(r)
+    b2 = gbr.Batch()
+    for r, s in zip(rs2, sl):
+        b2.add_scene(r, s)
+    b2.set_config(**best)
+    stream2 = torch.cuda.Stream(device=dev)
+    sets = [(b, rs, stream), (b2, rs2, stream2)]
+
+    def batch_e2e_steps(n):
+        for k in range(n):
+            bb, rr, ss = sets[k % 2]
+            sp = ss.cuda_stream
+            for r, h, s in zip(rr, hosts, sl):
+                r.update_vertices(0, h.data_ptr(), len(s.meshes[0].vertices), sp)
+            bb.render(sp)
+            if k > 0:
+                read_batch((k - 1) % 2)
+        read_batch((n - 1) % 2)
+
+    def read_batch(j):
+        bb, _, ss = sets[j]
+        for i, o in enumerate(outs[j]):
+            gbr.check(bb._lib.gbr_batch_readback(bb.h, i, gbr.C.c_void_p(o.data_ptr()), None, None,
+                                                 gbr.C.c_void_p(ss.cuda_stream)))
+
+    batch_e2e_steps(max(args.warmup, 2))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    batch_e2e_steps(args.steps)
+    torch.cuda.synchronize(dev)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    b2.close()
+    for r in rs2:
+        r.close()
     t_batch, t_e2e, t_seq = max_over_ranks([t_batch, t_e2e, t_seq], dist, dev)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

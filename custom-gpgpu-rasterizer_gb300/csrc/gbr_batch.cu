@@ -96,6 +96,7 @@ struct gbr_batch {
 
     // frame state
     bool have_frame = false;
+    bool frame_checked = false;   // finish_batch has waited for and checked the last frame
     cudaStream_t last_stream = nullptr;
     uint32_t overflow_reruns = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -393,6 +394,7 @@ gbr_status render_batch(gbr_batch* b, cudaStream_t s) {
         b->ev_recorded = true;
     }
     b->have_frame = true;
+    b->frame_checked = false;
     b->last_stream = s;
     return GBR_OK;
 }
@@ -400,6 +402,8 @@ gbr_status render_batch(gbr_batch* b, cudaStream_t s) {
 // Waits for the stream; re-renders with larger bin storage if the batch
 // outgrew it.
 gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
+    // the readbacks of a frame's scenes after the first find it complete
+    if (b->frame_checked) return GBR_OK;
     GBR_CUDA(cudaStreamSynchronize(s));
     GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     if (b->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
@@ -427,6 +431,7 @@ gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
         GBR_CUDA(cudaMemset(b->d_scan, 0, scan_state_bytes(b->total_bins)));
         return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the batch frame is invalid");
     }
+    b->frame_checked = true;
     return GBR_OK;
 }
 
