@@ -838,7 +838,8 @@ def profile_frames(n: int, binning: str = "exact", workload: str = "soup", batch
             rr.load_scene(s, CHUNK)
             rs.append(rr)
             b.add_scene(rr, s)
-        b.set_config(32, 2048, 6, 0)   # the autotuner's pick for these scenes
+        # the autotuner's pick for these scenes over the workload's space
+        b.set_config(32, 128, 5, 0, raster_threads=128)
         for _ in range(n):
             b.render()
         st = b.stats()
