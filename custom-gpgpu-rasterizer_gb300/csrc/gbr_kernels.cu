@@ -667,8 +667,12 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS * (kRasterThreads / THREADS)
             __syncthreads();   // the previous batch is done with the shared arrays
             S.bucket[tid] = 0u;
             __syncthreads();
+            // rows of THREADS entries up to the pass's n (uniform); entries at
+            // or past n are never read
+            const uint32_t rows = (n + THREADS - 1u) / THREADS;
 #pragma unroll 4
             for (uint32_t j = 0; j < kPer; ++j) {
+                if (j >= rows) break;
                 const uint32_t idx = j * THREADS + tid;
                 const uint32_t e = idx < n ? __ldg(list + start + b0 + idx) : kNoRasterBit;
                 const bool keep = !(e & kNoRasterBit);
@@ -703,6 +707,7 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS * (kRasterThreads / THREADS)
             __syncthreads();
 #pragma unroll
             for (uint32_t j = 0; j < kPer; ++j) {
+                if (j >= rows) break;
                 const uint32_t idx = j * THREADS + tid;
                 if (idx < n && !(S.prim[idx] & kNoRasterBit))
                     S.order[atomicAdd(&S.bucket[S.key[idx] >> kKeyShift], 1u)] = (uint16_t)idx;
