@@ -146,6 +146,9 @@ void free_bins(gbr_renderer* r) {
     r->items_cap = 0;
     r->list_cap = 0;
     r->seen_pairs = r->seen_visible = 0;
+    cudaFree(r->d_dirty);
+    r->d_dirty = nullptr;
+    r->dirty_valid = false;
 }
 
 gbr_status ensure_list(gbr_renderer* r, uint64_t pairs) {
@@ -311,6 +314,19 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     if (!F.flat_shade && vis != GBR_VIS_DEPTH) {
         if (!r->d_shade_list) GBR_CUDA(cudaMalloc(&r->d_shade_list, (size_t)r->W * r->H * sizeof(uint32_t)));
         F.shade_list = r->d_shade_list;
+        // the light pass leaves bins that stay clean untouched
+        if (r->d_dirty) {
+            uint8_t* rd = r->d_dirty + (size_t)r->dirty_parity * nb;
+            uint8_t* wr = r->d_dirty + (size_t)(r->dirty_parity ^ 1u) * nb;
+            if (!r->dirty_valid || r->dirty_vis != vis) GBR_CUDA(cudaMemsetAsync(rd, 1, nb, s));
+            F.dirty_rd = rd;
+            F.dirty_wr = wr;
+            r->dirty_parity ^= 1u;
+            r->dirty_valid = true;
+            r->dirty_vis = vis;
+        }
+    } else {
+        r->dirty_valid = false;   // one-pass shading writes every pixel
     }
 
     const bool stages = r->timing == GBR_TIMING_STAGES;
@@ -491,6 +507,7 @@ gbr_status gbr_setup_bins(gbr_renderer* r, uint32_t num_bins_x, uint32_t num_bin
     GBR_CUDA(cudaMalloc(&r->d_capacity, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMemset(r->d_capacity, 0, nb * sizeof(uint32_t)));
     GBR_CUDA(cudaMalloc(&r->d_bin_end, nb * sizeof(uint32_t)));
+    GBR_CUDA(cudaMalloc(&r->d_dirty, 2u * (size_t)nb));
     GBR_CUDA(cudaMalloc(&r->d_scan, scan_state_bytes(nb)));
     GBR_CUDA(cudaMemset(r->d_scan, 0, scan_state_bytes(nb)));
     GBR_CUDA(cudaMemset(r->d_bin_end, 0, nb * sizeof(uint32_t)));
@@ -682,6 +699,7 @@ gbr_status gbr_set_bin_rows(gbr_renderer* r, uint32_t row0, uint32_t row1) {
         return fail(GBR_ERR_INVALID_ARG, "bin rows [%u, %u) outside [0, %u)", row0, row1, r->nby);
     r->row0 = row0;
     r->row1 = row1;
+    r->dirty_valid = false;
     return GBR_OK;
 }
 

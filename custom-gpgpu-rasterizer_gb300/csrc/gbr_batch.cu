@@ -395,6 +395,7 @@ gbr_status render_batch(gbr_batch* b, cudaStream_t s) {
     }
     b->have_frame = true;
     b->frame_checked = false;
+    for (Member& m : b->members) m.r->dirty_valid = false;   // the batch rewrote their frame buffers
     b->last_stream = s;
     return GBR_OK;
 }

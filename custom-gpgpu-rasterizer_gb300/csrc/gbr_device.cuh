@@ -188,6 +188,13 @@ struct FrameDev {
     uint32_t px_begin, px_end;
     uint32_t rec_tma;          // raster: setup records staged by bulk asynchronous copies (1) or loads (0)
     uint32_t rows_pad[2];
+    // two-pass shading of a sparse frame: one byte per bin, "may hold drawn
+    // pixels".  dirty_rd: after the last frame; dirty_wr: this frame's, zeroed
+    // by its first scan and set by the raster for every bin it draws.  The
+    // light pass leaves the quads of bins clean in both untouched: their
+    // pixels already hold the clear values.  (null: every pixel is written)
+    uint8_t* dirty_rd;
+    uint8_t* dirty_wr;
 };
 static_assert(sizeof(FrameDev) % 16 == 0, "frame descriptors are copied as 16-byte words");
 
@@ -240,6 +247,7 @@ struct ScanDev {
     uint32_t mode;
     uint32_t spin_limit;           // polls of one flag before a look-back wait gives up (0: kScanSpinLimit)
     uint32_t silent_tile1;         // 1 + a tile that publishes nothing (0: none; test hook)
+    uint8_t* dirty;                // the frame's per-bin drawn flags to zero (FrameDev::dirty_wr; null: none)
 };
 
 // Many scenes rendered as one batch frame.  Each scene keeps its own frame

@@ -104,6 +104,7 @@ gbr_status gbr_draw_texture(gbr_renderer* r, int32_t tex_id, void* stream) {
     draw_texture_kernel<<<grid, block, 0, s>>>(r->d_colour, (cudaTextureObject_t)t->tex_obj, r->W, r->H);
     GBR_CUDA(cudaGetLastError());
     r->drawn = true;
+    r->dirty_valid = false;
     return GBR_OK;
 }
 
@@ -122,6 +123,7 @@ gbr_status gbr_draw_texture_global(gbr_renderer* r, int32_t tex_id, int stretch_
                                                                         r->W, r->H);
     GBR_CUDA(cudaGetLastError());
     r->drawn = true;
+    r->dirty_valid = false;
     return GBR_OK;
 }
 

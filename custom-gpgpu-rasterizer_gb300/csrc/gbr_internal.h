@@ -128,6 +128,16 @@ struct gbr_renderer {
     cudaEvent_t ev[5] = {};
     bool ev_recorded = false;
     uint32_t in_batches = 0;     // gbr_batch objects this renderer is a member of
+    // two-pass frames: per-bin "may hold drawn pixels" flags, two buffers of
+    // num_bins bytes alternating by frame (FrameDev::dirty_rd / dirty_wr).
+    // dirty_valid: they describe the frame buffers as the last frame left
+    // them, cleared for visualisation dirty_vis; any other writer of the
+    // buffers (one-pass frames, texture blits, batch frames, a new bin
+    // band) clears it, and the next two-pass frame marks every bin first.
+    uint8_t* d_dirty = nullptr;
+    uint32_t dirty_parity = 0;
+    bool dirty_valid = false;
+    uint32_t dirty_vis = 0;
 };
 
 namespace gbr {

@@ -636,6 +636,7 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS * (kRasterThreads / THREADS)
         __syncthreads();
         const uint32_t bin = S.item[0];
         if (bin == 0xFFFFFFFFu) break;
+        if (!BATCH && tid == 0 && F.dirty_wr) F.dirty_wr[bin] = 1u;   // the bin's pixels may now be drawn
         if (BATCH) {
             const uint32_t sc = S.scene_next;
             if (sc != S.scene_loaded) {   // uniform across the CTA
@@ -836,14 +837,46 @@ __global__ void __launch_bounds__(256) shade_kernel(FrameDev F) {
 // take per-pixel accesses.
 __global__ void __launch_bounds__(256) shade_queue_kernel(FrameDev F) {
     pdl_wait();
-    if (F.ctl->overflow) return;
+    if (F.ctl->overflow) {
+        // not rasterised: the buffers keep the last frame's pixels, and the
+        // next frame must find those bins as they were
+        if (F.dirty_rd)
+            for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < F.num_bins; b += gridDim.x * blockDim.x)
+                F.dirty_wr[b] |= F.dirty_rd[b];
+        return;
+    }
     // pixels [px_begin, px_end) (px_begin a multiple of 4)
     const uint32_t n = F.px_end ? F.px_end : F.width * F.height, lane = threadIdx.x & 31u;
     const uint32_t i0 = F.px_begin + (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
     const bool aligned = ((reinterpret_cast<uintptr_t>(F.gvis) | reinterpret_cast<uintptr_t>(F.colour) |
                            reinterpret_cast<uintptr_t>(F.depth) | reinterpret_cast<uintptr_t>(F.ids)) & 15u) == 0u;
+    // a quad whose pixels all lie in bins clean after the last frame and not
+    // drawn in this one already holds the clear values (pixels outside the
+    // bin grid are always written)
+    bool live = i0 < n;
+    if (live && F.dirty_rd) {
+        const uint32_t y = i0 / F.width, x = i0 - y * F.width;
+        if (x + 3u < F.width && i0 + 3u < n) {   // one row: bins [x / bw, (x + 3) / bw] of bin row y / bh
+            const bool p2 = ((F.bw & (F.bw - 1u)) | (F.bh & (F.bh - 1u))) == 0u;
+            const uint32_t sx = (uint32_t)__ffs((int)F.bw) - 1u, sy = (uint32_t)__ffs((int)F.bh) - 1u;
+            const uint32_t by = p2 ? y >> sy : y / F.bh;
+            const uint32_t bx0 = p2 ? x >> sx : x / F.bw, bx1 = p2 ? (x + 3u) >> sx : (x + 3u) / F.bw;
+            live = by >= F.nby || bx1 >= F.nbx;
+            for (uint32_t bx = bx0; !live && bx <= bx1; ++bx)
+                live = (F.dirty_rd[by * F.nbx + bx] | F.dirty_wr[by * F.nbx + bx]) != 0u;
+        } else {   // a quad that wraps a row, or the frame's last pixels
+            live = false;
+            const uint32_t last = min(i0 + 3u, n - 1u);
+            for (uint32_t i = i0; i <= last; ++i) {
+                const uint32_t yi = i / F.width, xi = i - yi * F.width;
+                const uint32_t bx = xi / F.bw, by = yi / F.bh;
+                live |= bx >= F.nbx || by >= F.nby || (F.dirty_rd[by * F.nbx + bx] | F.dirty_wr[by * F.nbx + bx]) != 0u;
+            }
+        }
+    }
     uint32_t covered = 0;   // bit k: pixel i0 + k has a winner
-    if (aligned && i0 + 4u <= n) {
+    if (!live) {
+    } else if (aligned && i0 + 4u <= n) {
         const ulonglong2* g = reinterpret_cast<const ulonglong2*>(F.gvis + i0);
         const ulonglong2 a = g[0], b = g[1];
         covered = (a.x != kEmptyVis ? 1u : 0u) | (a.y != kEmptyVis ? 2u : 0u) | (b.x != kEmptyVis ? 4u : 0u) |

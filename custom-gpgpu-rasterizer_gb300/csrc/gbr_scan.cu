@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(1024) scan_kernel(ScanDev S, uint32_t ntiles) 
     __shared__ unsigned long long s_excl[2];
     __shared__ uint32_t s_tile, s_tag;
     pdl_wait();
+    if (S.dirty)   // before any wait: a scan that gives up has still cleared them
+        for (uint32_t b = blockIdx.x * 1024u + threadIdx.x; b < S.n; b += gridDim.x * 1024u) S.dirty[b] = 0u;
     if (S.mode == kScanPredictedItems && S.feat) {
         // the pre-pass accumulators start the next frame empty (also when
         // this frame was flagged)
@@ -299,6 +301,9 @@ ScanDev scan_of(const FrameDev& F, uint32_t mode) {
     S.mode = mode;
     S.spin_limit = F.scan_spin_limit;
     S.silent_tile1 = F.scan_silent_tile1;
+    // the frame's first scan (exact, or the predicted capacities) clears
+    // the drawn flags the raster sets
+    S.dirty = mode == kScanExact || mode == kScanCapacity ? F.dirty_wr : nullptr;
     return S;
 }
 

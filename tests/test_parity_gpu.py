@@ -357,3 +357,40 @@ def test_tma_record_staging_renders_identically(gbr_lib, cuda_device, case, phas
         assert np.array_equal(out[0][key], out[1][key]), key
     ofx = oracle.render(s, oracle.RASTER_FIXED)
     assert_matches_fixed(out[1], ofx)
+
+
+def test_two_pass_frames_keep_clean_bins_clear(gbr_lib, cuda_device):
+    """Two-pass frames leave the light pass's quads in bins that were clean
+    after the last frame and are not drawn now untouched.  One renderer goes
+    through frames whose coverage grows, shrinks and moves, changes of view,
+    a one-pass depth frame and a texture blit; each frame equals a fresh
+    renderer's frame of the same camera and view, bit for bit."""
+    base = scenes.sphere_scene()   # textured: two-pass shading
+    W, H = base.width, base.height
+    cams = {"near": scenes.perspective_camera((0.0, 0.0, 2.2), 60.0, W, H),
+            "far": scenes.perspective_camera((0.0, 0.0, 9.0), 60.0, W, H),
+            "left": scenes.perspective_camera((1.6, 0.3, 3.5), 60.0, W, H)}
+    seq = [("near", scenes.VIS_PBR), ("far", scenes.VIS_PBR), ("left", scenes.VIS_PBR),
+           ("left", scenes.VIS_NORMAL), ("far", scenes.VIS_NORMAL), ("near", scenes.VIS_DEPTH),
+           ("far", scenes.VIS_PBR), ("blit", None), ("far", scenes.VIS_PBR), ("left", scenes.VIS_PBR)]
+
+    def frame(r, cam, vis):
+        base.camera, base.vis = cams[cam], vis
+        r.render_scene(base)
+        colour, depth = r.readback()
+        return colour.copy(), depth.view(np.uint32).copy(), r.readback_ids().copy()
+
+    r = gbr_lib.Renderer(W, H)
+    r.load_scene(base)
+    tex = r.add_texture(np.full((64, 64), 0xFFC8C8C8, np.uint32))
+    for cam, vis in seq:
+        if cam == "blit":
+            r.draw_texture(tex)
+            continue
+        got = frame(r, cam, vis)
+        with gbr_lib.Renderer(W, H) as fresh:
+            fresh.load_scene(base)
+            want = frame(fresh, cam, vis)
+        for name, a, b in zip(("colour", "depth", "ids"), got, want):
+            assert np.array_equal(a, b), f"{cam}/{vis}: {name} differs at {np.argwhere(a != b)[:3].tolist()}"
+    r.close()
