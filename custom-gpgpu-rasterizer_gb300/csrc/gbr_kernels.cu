@@ -854,9 +854,26 @@ __global__ void __launch_bounds__(256) shade_queue_kernel(FrameDev F) {
     // drawn in this one already holds the clear values (pixels outside the
     // bin grid are always written)
     bool live = i0 < n;
-    if (live && F.dirty_rd) {
-        const uint32_t y = i0 / F.width, x = i0 - y * F.width;
-        if (x + 3u < F.width && i0 + 3u < n) {   // one row: bins [x / bw, (x + 3) / bw] of bin row y / bh
+    if (F.dirty_rd) {
+        // the quad's row and column: one division per warp (its 32 quads
+        // are consecutive), then at most one row wrap per lane on frames at
+        // least 128 pixels wide
+        uint32_t y = 0, x = 0;
+        if (lane == 0u) {
+            y = i0 / F.width;
+            x = i0 - y * F.width;
+        }
+        y = __shfl_sync(0xFFFFFFFFu, y, 0);
+        x = __shfl_sync(0xFFFFFFFFu, x, 0) + 4u * lane;
+        if (F.width < 128u) {
+            y = i0 / F.width;
+            x = i0 - y * F.width;
+        } else if (x >= F.width) {
+            x -= F.width;
+            ++y;
+        }
+        if (!live) {
+        } else if (x + 3u < F.width && i0 + 3u < n) {   // one row: bins [x / bw, (x + 3) / bw] of bin row y / bh
             const bool p2 = ((F.bw & (F.bw - 1u)) | (F.bh & (F.bh - 1u))) == 0u;
             const uint32_t sx = (uint32_t)__ffs((int)F.bw) - 1u, sy = (uint32_t)__ffs((int)F.bh) - 1u;
             const uint32_t by = p2 ? y >> sy : y / F.bh;
@@ -873,6 +890,7 @@ __global__ void __launch_bounds__(256) shade_queue_kernel(FrameDev F) {
                 live |= bx >= F.nbx || by >= F.nby || (F.dirty_rd[by * F.nbx + bx] | F.dirty_wr[by * F.nbx + bx]) != 0u;
             }
         }
+        if (!__any_sync(0xFFFFFFFFu, live)) return;   // the warp's 128 pixels already hold the clear values
     }
     uint32_t covered = 0;   // bit k: pixel i0 + k has a winner
     if (!live) {
