@@ -271,6 +271,12 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         const uint64_t share = r->seen_pairs / (2u * grid);
         F.chunk = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(share, kMaxChunk), kMinChunk);
         if (F.phase == 0u) F.phase = r->seen_pairs < 4u * r->seen_visible ? kMaxPhase : kPhase;
+        // small triangles: about (pairs per visible triangle - 1) x the bin
+        // side of width + height each
+        if (F.phase >= kLanePhase && r->seen_visible) {
+            const double extent = ((double)r->seen_pairs / (double)r->seen_visible - 1.0) * 0.5 * (r->bw + r->bh);
+            F.raster_lanes = extent < kLaneExtentPx ? 1u : 0u;
+        }
     }
     F.raster_ctas = r->raster_ctas;
     F.meshes = r->d_meshes;
@@ -309,6 +315,7 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         F.count_split = 1u;
     }
     r->last_row_blocks = F.row_blocks;
+    r->last_raster_lanes = F.raster_lanes;
     // frames shaded through the full vertex stage shade their covered
     // pixels in a second, densely packed pass
     if (!F.flat_shade && vis != GBR_VIS_DEPTH) {
@@ -888,6 +895,7 @@ gbr_status gbr_get_stats(gbr_renderer* r, gbr_stats* out, void* stream) {
     out->predicted_overflow = r->h_ctl->pred_overflow;
     out->predicted_capacity = r->h_ctl->pred_capacity;
     out->count_blocks = r->last_row_blocks;
+    out->raster_lanes = r->last_raster_lanes;
     out->ms_setup = out->ms_bin = out->ms_raster = out->ms_shade = out->ms_total = 0.f;
     if (r->timing == GBR_TIMING_TOTAL && r->ev_recorded) {
         cudaEventElapsedTime(&out->ms_total, r->ev[0], r->ev[3]);

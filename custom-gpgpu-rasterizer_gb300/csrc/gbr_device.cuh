@@ -39,7 +39,17 @@ __host__ __device__ inline uint32_t count_split_for(unsigned long long pairs, ui
     const unsigned long long per_bin = pairs / (bins ? bins : 1u);
     return per_bin >= 256u ? 8u : per_bin >= 64u ? 4u : per_bin >= 16u ? 2u : 1u;
 }
-constexpr uint32_t kDefaultRasterCtas = 6;        // raster_kernel variant (CTAs per SM) used by default
+constexpr uint32_t kDefaultRasterCtas = 6;
+// The raster's small-triangle variant: in phases of at least kLanePhase
+// triangles a warp takes kLaneGrab sorted triangles at once and each lane
+// rasterises its own when its pixel box holds at most kLanePixels pixels.
+// The library picks it for sparse frames whose triangles span less than
+// kLaneExtentPx (width + height, estimated from the last frame's
+// (triangle, bin) pairs per visible triangle).
+constexpr uint32_t kLanePhase = 32;
+constexpr uint32_t kLaneGrab = 16;
+constexpr int kLanePixels = 16;
+constexpr double kLaneExtentPx = 16.0;        // raster_kernel variant (CTAs per SM) used by default
 // Exact binning with block-private counter rows: one block of kRowThreads
 // per SM counts its pairs per bin in shared memory (num_bins <=
 // kMaxRowBins), then takes its run of every bin it touched with one global
@@ -187,7 +197,8 @@ struct FrameDev {
     uint32_t row0, row1;
     uint32_t px_begin, px_end;
     uint32_t rec_tma;          // raster: setup records staged by bulk asynchronous copies (1) or loads (0)
-    uint32_t rows_pad[2];
+    uint32_t raster_lanes;     // raster: the small-triangle variant (a lane per triangle; phases >= kLanePhase)
+    uint32_t rows_pad;
     // two-pass shading of a sparse frame: one byte per bin, "may hold drawn
     // pixels".  dirty_rd: after the last frame; dirty_wr: this frame's, zeroed
     // by its first scan and set by the raster for every bin it draws.  The

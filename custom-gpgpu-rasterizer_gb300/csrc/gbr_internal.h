@@ -92,6 +92,7 @@ struct gbr_renderer {
     uint32_t* d_sub_base = nullptr;   // kCountSplit x bins
     uint32_t* d_row_base = nullptr;   // num_sms x bins (block-row exact binning; bins <= kMaxRowBins)
     uint32_t last_row_blocks = 0;     // blocks of the last frame's block-row count pass (0: sub-counters)
+    uint32_t last_raster_lanes = 0;   // the last frame's raster took the small-triangle variant
     uint32_t* d_offsets = nullptr;
     uint32_t* d_cursors = nullptr;
     uint32_t* d_capacity = nullptr;

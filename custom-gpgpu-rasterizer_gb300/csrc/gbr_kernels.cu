@@ -509,6 +509,42 @@ __device__ __forceinline__ void raster_fixed(const TriSetup& t, uint32_t prim, u
     }
 }
 
+// One lane's raster of a small triangle: raster_fixed's snapped box,
+// coverage, occlusion test, weights, depth and (key, id) minimum, pixel by
+// pixel (the edge functions evaluated exactly at each pixel equal the
+// stepped ones).  Returns false, having done nothing, for a triangle on the
+// float path or with a box of more than kLanePixels pixels.
+__device__ __forceinline__ bool raster_fixed_lane(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
+                                                  int ty0, int tw, int th, uint32_t key_bound) {
+    if (t.flags & kFlagFloat) return false;
+    const int X0 = snap_fx(t.x0), Y0 = snap_fx(t.y0), X1 = snap_fx(t.x1);
+    const int Y1 = snap_fx(t.y1), X2 = snap_fx(t.x2), Y2 = snap_fx(t.y2);
+    const int minx = min(X0, min(X1, X2)), maxx = max(X0, max(X1, X2));
+    const int miny = min(Y0, min(Y1, Y2)), maxy = max(Y0, max(Y1, Y2));
+    const int px0 = max((minx + 0xFFFF) >> kFxBits, tx0), px1 = min(maxx >> kFxBits, tx0 + tw - 1);
+    const int py0 = max((miny + 0xFFFF) >> kFxBits, ty0), py1 = min(maxy >> kFxBits, ty0 + th - 1);
+    if (px0 > px1 || py0 > py1) return true;
+    if ((px1 - px0 + 1) * (py1 - py0 + 1) > kLanePixels) return false;
+    for (int y = py0; y <= py1; ++y)
+        for (int x = px0; x <= px1; ++x) {
+            const int fx = x << kFxBits, fy = y << kFxBits;
+            if (edge_fx(fx, fy, X0, Y0, X1 - X0, Y1 - Y0) < 0 || edge_fx(fx, fy, X1, Y1, X2 - X1, Y2 - Y1) < 0 ||
+                edge_fx(fx, fy, X2, Y2, X0 - X2, Y0 - Y2) < 0)
+                continue;
+            unsigned long long* slot = tile + (y - ty0) * tw + (x - tx0);
+            const unsigned long long cur = *((volatile unsigned long long*)slot);
+            if ((uint32_t)(cur >> 32) < key_bound) continue;   // occluded
+            float w[3];
+            weights_fixed(t, x, y, w);
+            const float z = interp_z(w[0], w[1], w[2], t.z0, t.z1, t.z2);
+            if (!(z >= 0.f && z < 1.f)) continue;
+            const uint32_t key = (uint32_t)__float2int_rz(__fmul_rn(z, 2147483648.0f));
+            const unsigned long long packed = ((unsigned long long)key << 32) | prim;
+            if (packed < cur) atomicMin(slot, packed);
+        }
+    return true;
+}
+
 // Triangles outside the guard band: the reference's float edge functions.
 __device__ __noinline__ void raster_float(const TriSetup& t, uint32_t prim, unsigned long long* tile, int tx0,
                                              int ty0, int tw, int th, uint32_t lane) {
@@ -587,7 +623,9 @@ __device__ __forceinline__ void fetch_item(uint4* dst, const uint4* items, uint3
 // memory when it differs from the previous item's.
 // MIN_CTAS counts CTAs of 256 threads: a 128-thread variant keeps twice as
 // many resident (the same registers per thread).
-template <int MIN_CTAS, bool BATCH, bool TMA = false, int THREADS = kRasterThreads>
+// LANES: the small-triangle variant (kLanePhase), a kernel of its own so
+// that the one-triangle-per-warp path keeps its registers.
+template <int MIN_CTAS, bool BATCH, bool TMA = false, int THREADS = kRasterThreads, bool LANES = false>
 __global__ void __launch_bounds__(THREADS, MIN_CTAS * (kRasterThreads / THREADS)) raster_kernel(FrameDev F, BatchDev B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Shared = RasterSharedT<THREADS>;
@@ -775,16 +813,38 @@ __global__ void __launch_bounds__(THREADS, MIN_CTAS * (kRasterThreads / THREADS)
                     break;
                 }
                 const uint32_t p1 = min(limit, p0 + phase);
+                // a warp takes one sorted triangle at a time; the
+                // small-triangle variant takes kLaneGrab in phases of at least
+                // kLanePhase triangles, each lane rasterises its own when its
+                // pixel box holds at most kLanePixels pixels, and the warp the
+                // others
+                const bool lanes = LANES && phase >= kLanePhase;
                 for (;;) {
-                    int k = 0;
-                    if (lane == 0) k = atomicAdd(&S.next, 1);
-                    k = __shfl_sync(0xFFFFFFFFu, k, 0);
-                    if (k >= (int)p1) break;
-                    const uint32_t i = S.order[k];
-                    if (S.key[i] > tile_max) continue;
-                    const TriSetup& t = S.rec[(uint32_t)k & (kMaxPhase - 1u)];
-                    if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
-                    else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane, S.key[i]);
+                    int kb = 0;
+                    if (lane == 0) kb = atomicAdd(&S.next, lanes ? (int)kLaneGrab : 1);
+                    kb = __shfl_sync(0xFFFFFFFFu, kb, 0);
+                    if (kb >= (int)p1) break;
+                    uint32_t m;   // bit l: triangle kb + l goes to the whole warp
+                    if (lanes) {
+                        const uint32_t k = (uint32_t)kb + lane;
+                        bool big = false;
+                        if (lane < kLaneGrab && k < p1) {
+                            const uint32_t i = S.order[k];
+                            const uint32_t key = S.key[i];
+                            if (key <= tile_max)
+                                big = !raster_fixed_lane(S.rec[k & (kMaxPhase - 1u)], S.prim[i], tile, tx0, ty0, tw, th,
+                                                         key);
+                        }
+                        m = __ballot_sync(0xFFFFFFFFu, big);
+                    } else {
+                        m = S.key[S.order[kb]] <= tile_max ? 1u : 0u;
+                    }
+                    for (; m; m &= m - 1u) {
+                        const uint32_t k = (uint32_t)kb + (uint32_t)(__ffs(m) - 1), i = S.order[k];
+                        const TriSetup& t = S.rec[k & (kMaxPhase - 1u)];
+                        if (t.flags & kFlagFloat) raster_float(t, S.prim[i], tile, tx0, ty0, tw, th, lane);
+                        else raster_fixed(t, S.prim[i], tile, tx0, ty0, tw, th, lane, S.key[i]);
+                    }
                 }
             }
         }
@@ -1121,24 +1181,26 @@ cudaError_t launch_fill(const FrameDev& F, cudaStream_t s) {
     return launch_pdl(fill_kernel, dim3(blocks), dim3(256), 0, s, F);
 }
 
-template <bool BATCH, bool TMA = false, int THREADS = kRasterThreads>
+template <bool BATCH, bool TMA = false, int THREADS = kRasterThreads, bool LANES = false>
 static cudaError_t launch_raster_variant(const FrameDev& F, const BatchDev& B, uint32_t ctas, uint32_t grid, size_t smem,
                                          cudaStream_t s) {
     const dim3 g(grid), b(THREADS);
     switch (ctas ? ctas : kDefaultRasterCtas) {
-        case 2: return launch_pdl(raster_kernel<2, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
-        case 3: return launch_pdl(raster_kernel<3, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
-        case 5: return launch_pdl(raster_kernel<5, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
-        case 6: return launch_pdl(raster_kernel<6, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
-        default: return launch_pdl(raster_kernel<4, BATCH, TMA, THREADS>, g, b, smem, s, F, B);
+        case 2: return launch_pdl(raster_kernel<2, BATCH, TMA, THREADS, LANES>, g, b, smem, s, F, B);
+        case 3: return launch_pdl(raster_kernel<3, BATCH, TMA, THREADS, LANES>, g, b, smem, s, F, B);
+        case 5: return launch_pdl(raster_kernel<5, BATCH, TMA, THREADS, LANES>, g, b, smem, s, F, B);
+        case 6: return launch_pdl(raster_kernel<6, BATCH, TMA, THREADS, LANES>, g, b, smem, s, F, B);
+        default: return launch_pdl(raster_kernel<4, BATCH, TMA, THREADS, LANES>, g, b, smem, s, F, B);
     }
 }
 
 cudaError_t launch_raster(const FrameDev& F, uint32_t grid, cudaStream_t s) {
     BatchDev none;
     memset(&none, 0, sizeof none);
-    return F.rec_tma ? launch_raster_variant<false, true>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s)
-                     : launch_raster_variant<false>(F, none, F.raster_ctas, grid, raster_smem_bytes(F.bw, F.bh), s);
+    const size_t smem = raster_smem_bytes(F.bw, F.bh);
+    if (F.rec_tma) return launch_raster_variant<false, true>(F, none, F.raster_ctas, grid, smem, s);
+    if (F.raster_lanes) return launch_raster_variant<false, false, kRasterThreads, true>(F, none, F.raster_ctas, grid, smem, s);
+    return launch_raster_variant<false>(F, none, F.raster_ctas, grid, smem, s);
 }
 
 cudaError_t launch_shade(const FrameDev& F, cudaStream_t s) {
@@ -1195,8 +1257,11 @@ static cudaError_t configure_variant(size_t smem, int* blocks_per_sm) {
     cudaError_t e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, BATCH, false, THREADS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (!BATCH) {   // the bulk-copy staging variant of a single frame
+    if (!BATCH) {   // the bulk-copy staging and small-triangle variants of a single frame
         e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(raster_kernel<MIN_CTAS, false, false, kRasterThreads, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, raster_kernel<MIN_CTAS, BATCH, false, THREADS>,

@@ -57,7 +57,8 @@ class Stats(C.Structure):
                 ("overflow_reruns", C.c_uint32), ("predicted_overflow", C.c_uint32),
                 ("predicted_capacity", C.c_uint64),
                 ("ms_setup", C.c_float), ("ms_bin", C.c_float), ("ms_raster", C.c_float), ("ms_total", C.c_float),
-                ("ms_shade", C.c_float), ("count_blocks", C.c_uint32)]
+                ("ms_shade", C.c_float), ("count_blocks", C.c_uint32), ("raster_lanes", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class Light(C.Structure):

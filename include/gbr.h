@@ -79,6 +79,9 @@ typedef struct {
     float ms_shade;              /* the shade pass (included in ms_total, not in ms_raster) */
     uint32_t count_blocks;       /* blocks with private counter rows in the last frame's exact
                                     count pass (0: per-bin counters in global memory) */
+    uint32_t raster_lanes;       /* 1: the last frame's raster took its small-triangle variant (a lane
+                                    per triangle; picked for sparse frames of small triangles) */
+    uint32_t reserved;
 } gbr_stats;
 
 /* CUDARenderer(const WindowHelper&) (CUDARenderer.cu:33-46): headless, the

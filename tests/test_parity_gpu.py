@@ -221,8 +221,11 @@ def test_icosphere_4k_subpixel(gbr_lib, cuda_device, bins):
     triangles, 8x8 and 16x16 bins (the reference's 8x8 bins rasterise nothing,
     so 8x8 is checked against the oracle only)."""
     s = scenes.icosphere_scene(bin_size=bins)
-    g, o = run_case(gbr_lib, s, ref_band=(bins == 16))
+    # the second frame takes the raster's small-triangle variant (a lane per
+    # triangle), chosen from the first frame's pairs per visible triangle
+    g, o = run_case(gbr_lib, s, ref_band=(bins == 16), frames=2)
     assert g["stats"]["num_visible"] > 100_000 and (g["ids"] != EMPTY).sum() > 100_000
+    assert g["stats"]["raster_lanes"] == 1
 
 
 @pytest.mark.parametrize("lights", [False, True])
@@ -393,4 +396,32 @@ def test_two_pass_frames_keep_clean_bins_clear(gbr_lib, cuda_device):
             want = frame(fresh, cam, vis)
         for name, a, b in zip(("colour", "depth", "ids"), got, want):
             assert np.array_equal(a, b), f"{cam}/{vis}: {name} differs at {np.argwhere(a != b)[:3].tolist()}"
+    r.close()
+
+
+def test_small_triangle_variant_is_chosen_from_the_last_frame(gbr_lib, cuda_device):
+    """The raster's small-triangle variant (a lane per triangle) follows the
+    last frame's (triangle, bin) pairs per visible triangle: the 640x480
+    sphere's ~10-pixel triangles keep one triangle per warp, a frame of
+    sub-pixel triangles takes the variant, the first frame of a renderer
+    (no history) and an explicit phase below 32 never do; the frames are
+    the fixed-mode oracle's either way."""
+    sphere = scenes.sphere_scene()
+    g = gpu_render(gbr_lib, sphere, frames=2)
+    assert g["stats"]["raster_lanes"] == 0
+    g["renderer"].close()
+    s = scenes.icosphere_scene(640, 480, bin_size=16, subdiv=6)
+    ofx = oracle.render(s, oracle.RASTER_FIXED)
+    first = gpu_render(gbr_lib, s, frames=1)
+    assert first["stats"]["raster_lanes"] == 0
+    first["renderer"].close()
+    g = gpu_render(gbr_lib, s, frames=2)
+    assert g["stats"]["raster_lanes"] == 1
+    assert_matches_fixed(g, ofx)
+    g["renderer"].close()
+    r = gbr_lib.Renderer(s.width, s.height)
+    r.set_raster_params(16, 0)
+    g = gpu_render(gbr_lib, s, renderer=r, frames=2)
+    assert g["stats"]["raster_lanes"] == 0
+    assert_matches_fixed(g, ofx)
     r.close()
