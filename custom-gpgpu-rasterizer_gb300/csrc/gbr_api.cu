@@ -270,12 +270,15 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
         const uint64_t grid = (uint64_t)r->num_sms * (uint64_t)std::max(r->raster_blocks_per_sm, 1);
         const uint64_t share = r->seen_pairs / (2u * grid);
         F.chunk = (uint32_t)std::max<uint64_t>(std::min<uint64_t>(share, kMaxChunk), kMinChunk);
-        if (F.phase == 0u) F.phase = r->seen_pairs < 4u * r->seen_visible ? kMaxPhase : kPhase;
+        if (F.phase == 0u) F.phase = r->seen_pairs < 4u * r->seen_visible ? kSparsePhase : kPhase;
         // small triangles: about (pairs per visible triangle - 1) x the bin
-        // side of width + height each
+        // side of width + height each; with the library's phase the
+        // small-triangle variant runs phases of the whole record ring, so
+        // that every warp of the CTA takes a share of each phase
         if (F.phase >= kLanePhase && r->seen_visible) {
             const double extent = ((double)r->seen_pairs / (double)r->seen_visible - 1.0) * 0.5 * (r->bw + r->bh);
             F.raster_lanes = extent < kLaneExtentPx ? 1u : 0u;
+            if (F.raster_lanes && r->raster_phase == 0u) F.phase = kMaxPhase;
         }
     }
     F.raster_ctas = r->raster_ctas;

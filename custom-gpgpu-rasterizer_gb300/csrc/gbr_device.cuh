@@ -25,7 +25,8 @@ constexpr int kRasterThreads = 256;
 constexpr int kBatch = 2048;                      // bin entries the raster depth-sorts at once
 constexpr int kDepthBuckets = 256;                // front-to-back buckets: top 8 bits of the depth key
 constexpr uint32_t kPhase = 16;                   // triangles between hierarchical-z refreshes
-constexpr uint32_t kMaxPhase = 64;                // setup records staged per phase
+constexpr uint32_t kMaxPhase = 128;               // setup records staged per phase (the record ring)
+constexpr uint32_t kSparsePhase = 64;             // the library's phase for frames of small triangles
 constexpr uint32_t kMinChunk = 64;                // smallest raster work item the library picks
 constexpr uint32_t kMaxChunk = 4096;              // largest raster work item the library picks
 constexpr uint32_t kBatchChunk = 2048;            // raster work items of a batch frame

@@ -221,7 +221,8 @@ gbr_status gbr_set_lights(gbr_renderer *r, const gbr_light *lights, uint32_t n);
 /* Binning method for the following frames. */
 gbr_status gbr_set_binning(gbr_renderer *r, uint32_t method);
 /* Raster tuning (no counterpart in the reference; used by the autotuner):
- * phase = triangles rasterised between hierarchical-z refreshes, 0..64 (0: 16),
+ * phase = triangles rasterised between hierarchical-z refreshes, 0..128 (0: the library's choice: 16,
+ * 64 for frames of small triangles, 128 with the raster's small-triangle variant),
  * ctas_per_sm = occupancy variant of the raster kernel, 2..6 (0: 6). */
 gbr_status gbr_set_raster_params(gbr_renderer *r, uint32_t phase, uint32_t ctas_per_sm);
 /* How the raster stages triangle-setup records into shared memory (no
@@ -298,7 +299,7 @@ typedef struct {
     uint32_t queue_chunk;  /* entries depth-sorted and rasterised per pass over a tile, >= 1 (at most 2048
                               used); work items hold 2048 entries */
     uint32_t raster_ctas;  /* raster variant: CTAs per SM, 2..6 (0: 6), counted in CTAs of 256 threads */
-    uint32_t raster_phase; /* triangles between hierarchical-z refreshes, 0..64 (0: 16) */
+    uint32_t raster_phase; /* triangles between hierarchical-z refreshes, 0..128 (0: 16) */
     uint32_t raster_threads; /* threads per bin: raster CTAs of 128 or 256 threads (0: 256); a 128-thread CTA
                                 depth-sorts 1024 entries at a time into 128 buckets, and twice raster_ctas
                                 of them are resident per SM */
