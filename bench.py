@@ -764,11 +764,9 @@ def run_batch(args, rank, world, local, nested=False, dist=None):
                 read_batch((k - 1) % 2)
         read_batch((n - 1) % 2)
 
-    def read_batch(j):
+    def read_batch(j):   # every scene's colours, one wait
         bb, _, ss = sets[j]
-        for i, o in enumerate(outs[j]):
-            gbr.check(bb._lib.gbr_batch_readback(bb.h, i, gbr.C.c_void_p(o.data_ptr()), None, None,
-                                                 gbr.C.c_void_p(ss.cuda_stream)))
+        bb.readback_all([o.data_ptr() for o in outs[j]], stream=ss.cuda_stream)
 
     batch_e2e_steps(max(args.warmup, 2))
     torch.cuda.synchronize(dev)

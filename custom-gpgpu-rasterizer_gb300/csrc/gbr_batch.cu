@@ -663,6 +663,21 @@ gbr_status gbr_batch_readback(gbr_batch* b, uint32_t index, uint32_t* colour, fl
     return GBR_OK;
 }
 
+gbr_status gbr_batch_readback_all(gbr_batch* b, uint32_t* const* colours, void* stream) {
+    if (!b || !colours) return fail(GBR_ERR_INVALID_ARG, "null argument");
+    if (!b->have_frame) return fail(GBR_ERR_INVALID_ARG, "no batch frame rendered");
+    cudaStream_t s = (cudaStream_t)stream;
+    gbr_status st = finish_batch(b, s);
+    if (st != GBR_OK) return st;
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        if (!colours[i]) continue;
+        const gbr_renderer* r = b->members[i].r;
+        GBR_CUDA(cudaMemcpyAsync(colours[i], r->d_colour, (size_t)r->W * r->H * 4u, cudaMemcpyDeviceToHost, s));
+    }
+    GBR_CUDA(cudaStreamSynchronize(s));
+    return GBR_OK;
+}
+
 gbr_status gbr_batch_get_bins(gbr_batch* b, uint32_t index, uint32_t* offsets, uint32_t* ids, uint64_t capacity,
                               uint64_t* num_pairs, void* stream) {
     if (!b || index >= b->members.size()) return fail(GBR_ERR_INVALID_ARG, "bad batch or index");

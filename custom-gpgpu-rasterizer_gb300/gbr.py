@@ -37,7 +37,7 @@ EXPORTED = ["gbr_create", "gbr_destroy", "gbr_setup_bins", "gbr_mesh_upload", "g
             "gbr_get_bins", "gbr_get_stats", "gbr_batch_create", "gbr_batch_destroy", "gbr_batch_add",
             "gbr_batch_set_view", "gbr_batch_set_config", "gbr_batch_get_config", "gbr_batch_autotune",
             "gbr_batch_set_timing", "gbr_batch_render", "gbr_batch_get_stats", "gbr_batch_scene_bins",
-            "gbr_batch_readback", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_draw_texture", "gbr_draw_texture_global", "gbr_obj_read_file", "gbr_obj_read_text",
+            "gbr_batch_readback", "gbr_batch_readback_all", "gbr_batch_get_bins", "gbr_render_noalloc", "gbr_draw_texture", "gbr_draw_texture_global", "gbr_obj_read_file", "gbr_obj_read_text",
             "gbr_obj_free", "gbr_last_error_string", "gbr_version"]
 
 
@@ -142,6 +142,7 @@ def lib():
             "gbr_batch_get_stats": [vp, C.POINTER(BatchStats), vp],
             "gbr_batch_scene_bins": [vp, u32, C.POINTER(u32), C.POINTER(u32)],
             "gbr_batch_readback": [vp, u32, vp, vp, vp, vp],
+            "gbr_batch_readback_all": [vp, vp, vp],
             "gbr_batch_get_bins": [vp, u32, vp, vp, u64, C.POINTER(u64), vp],
             "gbr_draw_texture": [vp, C.c_int32, vp],
             "gbr_draw_texture_global": [vp, C.c_int32, C.c_int, u32, vp],
@@ -487,6 +488,18 @@ class Batch:
         check(self._lib.gbr_batch_readback(self.h, index, _ptr(colour), _ptr(depth), _ptr(ids), _stream(stream)))
         shp = (r.height, r.width)
         return colour.reshape(shp), depth.reshape(shp), ids.reshape(shp)
+
+    def readback_all(self, colours=None, stream: int = 0):
+        """Every scene's colour buffer, [height, width] each, with one wait:
+        into `colours` (arrays of the scenes' sizes, or host pointers; None
+        entries are skipped) or into new arrays."""
+        if colours is None:
+            colours = [np.empty(r.width * r.height, np.uint32) for r in self.renderers]
+        ptrs = (C.c_void_p * len(colours))(*[None if c is None else (c if isinstance(c, int) else _ptr(c))
+                                              for c in colours])
+        check(self._lib.gbr_batch_readback_all(self.h, ptrs, _stream(stream)))
+        return [c.reshape(r.height, r.width) if isinstance(c, np.ndarray) else c
+                for c, r in zip(colours, self.renderers)]
 
     def get_bins(self, index: int, stream: int = 0):
         """(offsets[num_bins+1], ids) of scene `index`; ids sorted within each bin."""

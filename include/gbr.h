@@ -344,6 +344,10 @@ gbr_status gbr_batch_scene_bins(const gbr_batch *b, uint32_t index, uint32_t *nu
  * last batch frame (any output pointer may be NULL). */
 gbr_status gbr_batch_readback(gbr_batch *b, uint32_t index, uint32_t *colour, float *depth, uint32_t *ids,
                               void *stream);
+/* The colour buffers of every scene of the last batch frame: colours[i]
+ * (NULL: skipped) gets scene i's framebuffer; the copies are queued on
+ * `stream` together and waited for once. */
+gbr_status gbr_batch_readback_all(gbr_batch *b, uint32_t *const *colours, void *stream);
 gbr_status gbr_batch_get_bins(gbr_batch *b, uint32_t index, uint32_t *offsets, uint32_t *ids, uint64_t capacity,
                               uint64_t *num_pairs, void *stream);
 

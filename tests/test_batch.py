@@ -194,6 +194,23 @@ def test_batch_autotune_keeps_output(gbr_lib, cuda_device):
 
 
 @pytest.mark.gpu
+def test_batch_readback_all_equals_per_scene_readback(gbr_lib, cuda_device):
+    sl = scenes.batch_scenes(6, seed=4, max_tris=20000)
+    b, rs = build_batch(gbr_lib, sl)
+    b.set_config(16, 64)
+    b.render()
+    every = b.readback_all()
+    some = [np.zeros(s.width * s.height, np.uint32) if i % 2 == 0 else None for i, s in enumerate(sl)]
+    b.readback_all(some)
+    for i in range(len(sl)):
+        colour = b.readback(i)[0]
+        assert np.array_equal(every[i], colour)
+        if some[i] is not None:
+            assert np.array_equal(some[i].reshape(colour.shape), colour)
+    close_batch(b, rs)
+
+
+@pytest.mark.gpu
 def test_renderer_in_batch_cannot_be_destroyed(gbr_lib, cuda_device):
     s = scenes.soup_scene(1000, 256, 256, seed=1)
     b, rs = build_batch(gbr_lib, [s])
