@@ -261,8 +261,9 @@ gbr_status render_frame(gbr_renderer* r, const gbr_camera* cam, uint32_t cull, u
     // serialise the frame), within [kMinChunk, kMaxChunk]; queue_chunk is
     // the pass size (entries depth-sorted and rasterised at a time); with the
     // library's phase, triangles spanning under 4 bins on average (little
-    // overdraw per bin) refresh the tile's depth bound every kMaxPhase
-    // triangles rather than every kPhase
+    // overdraw per bin) refresh the tile's depth bound every kSparsePhase
+    // triangles rather than every kPhase (every kMaxPhase with the
+    // small-triangle variant, below)
     F.chunk = kMaxChunk;
     F.stage = r->chunk;   // queue_chunk: entries per raster pass
     F.phase = r->raster_phase;
