@@ -404,8 +404,8 @@ gbr_status scan_timed_out(gbr_renderer* r) {
 // Waits for the stream; re-renders with larger bin storage if the frame
 // overflowed it.
 gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
+    GBR_CUDA(cudaMemcpyAsync(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));   // pinned: one wait
     GBR_CUDA(cudaStreamSynchronize(s));
-    GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     // a bounded wait that gave up flags the frame before any storage check
     // (its overflow flag only stopped the kernels after the scan)
     if (r->h_ctl->error) return scan_timed_out(r);
@@ -416,8 +416,8 @@ gbr_status finish_frame(gbr_renderer* r, cudaStream_t s) {
         ++r->overflow_reruns;
         st = render_frame(r, &r->last_cam, r->last_cull, r->last_sample, r->last_vis, s);
         if (st != GBR_OK) return st;
+        GBR_CUDA(cudaMemcpyAsync(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));   // pinned: one wait
         GBR_CUDA(cudaStreamSynchronize(s));
-        GBR_CUDA(cudaMemcpy(r->h_ctl, r->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
         if (r->h_ctl->error) return scan_timed_out(r);
     }
     if (r->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "bin storage overflow persists");

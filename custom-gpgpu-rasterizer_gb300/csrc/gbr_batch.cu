@@ -405,8 +405,8 @@ gbr_status render_batch(gbr_batch* b, cudaStream_t s) {
 gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
     // the readbacks of a frame's scenes after the first find it complete
     if (b->frame_checked) return GBR_OK;
+    GBR_CUDA(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));   // pinned: one wait
     GBR_CUDA(cudaStreamSynchronize(s));
-    GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     if (b->h_ctl->error) {   // a bounded wait of the bin scan gave up: restart its state
         GBR_CUDA(cudaMemset(b->d_scan, 0, scan_state_bytes(b->total_bins)));
         return fail(GBR_ERR_TIMEOUT, "bin scan wait timed out; the batch frame is invalid");
@@ -417,8 +417,8 @@ gbr_status finish_batch(gbr_batch* b, cudaStream_t s) {
         ++b->overflow_reruns;
         st = render_batch(b, s);
         if (st != GBR_OK) return st;
+        GBR_CUDA(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));   // pinned: one wait
         GBR_CUDA(cudaStreamSynchronize(s));
-        GBR_CUDA(cudaMemcpy(b->h_ctl, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     }
     if (b->h_ctl->overflow) return fail(GBR_ERR_OUT_OF_MEMORY, "batch bin storage overflow persists");
     // sub-counters per bin for the next frames, from this frame's density
